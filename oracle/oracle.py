@@ -1,0 +1,445 @@
+"""ctypes loader for the CPU checkers (TEST INFRASTRUCTURE ONLY).
+
+Two libraries share one ABI (oracle/mvs_oracle.h):
+  * liboracle.so        -- the C restatement of the reference MVS path
+                           (oracle/mvs_oracle.c), built here and on any host;
+  * _ref/libref_mvs.so  -- the reference's own sources compiled as they are
+                           (oracle/ref_wrapper.cpp), only where the reference
+                           tree is present.
+
+Only tests/, __graft_entry__.smoke() and bench.py (CPU baseline and the
+reference arm) may import this module.  The GPU engine never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_mvs.so")
+REFERENCE_TREE = "/root/reference"
+
+
+class Intrinsics(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fx", "fy", "cx", "cy", "k1", "k2", "k3", "p1", "p2", "width", "height")]
+
+
+class Pose(C.Structure):
+    _fields_ = [("r", C.c_double * 9), ("t", C.c_double * 3), ("timestamp_ns", C.c_double)]
+
+
+# recon::MvsConfig (core/include/recon/mvs.h:24-67), defaults included.
+_CONFIG_FIELDS = [
+    ("num_views", C.c_int32, 7), ("ref_view_index", C.c_int32, -1),
+    ("ideal_angle_min_deg", C.c_double, 8.0), ("ideal_angle_max_deg", C.c_double, 35.0),
+    ("max_view_scale_mismatch", C.c_double, 0.15), ("view_angle_weight", C.c_double, 1.0),
+    ("view_texture_weight", C.c_double, 0.8), ("view_spread_weight", C.c_double, 0.6),
+    ("view_scale_weight", C.c_double, 0.4), ("reference_depth_m", C.c_double, 0.40),
+    ("patch_size", C.c_int32, 11), ("iterations", C.c_int32, 4), ("random_search_count", C.c_int32, 5),
+    ("random_search_radius_ratio", C.c_double, 0.30), ("restart_ratio", C.c_double, 0.05),
+    ("propagation_directions", C.c_int32, 4), ("propagation_enabled", C.c_int32, 1),
+    ("num_threads", C.c_int32, 0), ("photo_threshold", C.c_double, 1.0),
+    ("depth_regularization", C.c_double, 0.02), ("geo_consistency_threshold", C.c_double, 0.02),
+    ("weak_texture_variance", C.c_double, 12.0), ("subpixel_iterations", C.c_int32, 4),
+    ("subpixel_fit_points", C.c_int32, 5), ("subpixel_window_ratio", C.c_double, 0.005),
+    ("min_depth_m", C.c_double, 0.10), ("max_depth_m", C.c_double, 1.50),
+    ("min_view_consistency", C.c_int32, 2), ("fusion_voxel_size_m", C.c_double, 0.001),
+]
+CONFIG_DEFAULTS = {n: d for n, _, d in _CONFIG_FIELDS}
+
+
+class Config(C.Structure):
+    _fields_ = [(n, t) for n, t, _ in _CONFIG_FIELDS]
+
+
+def make_config(**overrides) -> Config:
+    c = Config()
+    for n, _, d in _CONFIG_FIELDS:
+        setattr(c, n, overrides.get(n, d))
+    unknown = set(overrides) - set(CONFIG_DEFAULTS)
+    if unknown:
+        raise KeyError(f"unknown MvsConfig fields: {sorted(unknown)}")
+    return c
+
+
+class Views(C.Structure):
+    _fields_ = [
+        ("ref", C.POINTER(C.c_uint8)), ("ref_w", C.c_int32), ("ref_h", C.c_int32),
+        ("num_src", C.c_int32), ("src", C.POINTER(C.POINTER(C.c_uint8))),
+        ("src_w", C.POINTER(C.c_int32)), ("src_h", C.POINTER(C.c_int32)),
+        ("ref_pose", C.POINTER(Pose)), ("src_poses", C.POINTER(Pose)), ("num_src_poses", C.c_int32),
+        ("ref_intr", C.POINTER(Intrinsics)), ("src_intr", C.POINTER(Intrinsics)), ("num_src_intr", C.c_int32),
+        ("source_indices", C.POINTER(C.c_int32)),
+    ]
+
+
+class NccResult(C.Structure):
+    _fields_ = [("valid", C.c_int32), ("ncc", C.c_double), ("weak_texture", C.c_int32), ("valid_samples", C.c_int32)]
+
+
+class DepthMapC(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("depth", C.POINTER(C.c_float)),
+                ("support_count", C.POINTER(C.c_uint8)), ("confidence", C.POINTER(C.c_float))]
+
+
+class ConsistencyParams(C.Structure):
+    _fields_ = [("rel_depth_max", C.c_float), ("reproj_px_max", C.c_float), ("min_views", C.c_int32)]
+
+
+def intrinsics_from(arr) -> Intrinsics:
+    a = np.asarray(arr, np.float64)
+    return Intrinsics(*a.tolist())
+
+
+def pose_from(arr) -> Pose:
+    a = np.asarray(arr, np.float64)
+    p = Pose()
+    for i in range(9):
+        p.r[i] = a[i]
+    for i in range(3):
+        p.t[i] = a[9 + i]
+    p.timestamp_ns = a[12] if a.size > 12 else 0.0
+    return p
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class ViewSet:
+    """Keeps the numpy buffers of one PatchMatchStereo call alive and exposes
+    them as an orc_views struct.  `cams` are synthetic.Camera objects (or any
+    object with intrinsics_array()/pose_array()); poses are passed as a
+    global array with intrinsics in relative form by default."""
+
+    def __init__(self, ref_img, src_imgs, ref_cam, src_cams, source_indices=None,
+                 all_poses=None, intrinsics="relative"):
+        self.ref = np.ascontiguousarray(ref_img, np.uint8)
+        self.srcs = [np.ascontiguousarray(s, np.uint8) for s in src_imgs]
+        n = len(self.srcs)
+        if all_poses is None:
+            all_poses = [c.pose_array() for c in src_cams]
+            source_indices = list(range(n)) if source_indices is None else source_indices
+        self.source_indices = np.asarray(source_indices, np.int32)
+        self.poses = (Pose * len(all_poses))(*[pose_from(p) for p in all_poses])
+        if intrinsics == "relative":
+            intr = [c.intrinsics_array() for c in src_cams]
+        else:
+            intr = intrinsics
+        self.intr = (Intrinsics * len(intr))(*[intrinsics_from(k) for k in intr])
+        self.ref_pose = pose_from(ref_cam.pose_array())
+        self.ref_intr = intrinsics_from(ref_cam.intrinsics_array())
+        self.src_ptrs = (C.POINTER(C.c_uint8) * n)(*[_ptr(s, C.c_uint8) for s in self.srcs])
+        self.src_w = np.asarray([s.shape[1] for s in self.srcs], np.int32)
+        self.src_h = np.asarray([s.shape[0] for s in self.srcs], np.int32)
+        self.struct = Views(
+            _ptr(self.ref, C.c_uint8), self.ref.shape[1], self.ref.shape[0], n,
+            C.cast(self.src_ptrs, C.POINTER(C.POINTER(C.c_uint8))),
+            _ptr(self.src_w, C.c_int32), _ptr(self.src_h, C.c_int32),
+            C.pointer(self.ref_pose), C.cast(self.poses, C.POINTER(Pose)), len(all_poses),
+            C.pointer(self.ref_intr), C.cast(self.intr, C.POINTER(Intrinsics)), len(intr),
+            _ptr(self.source_indices, C.c_int32))
+
+    @property
+    def shape(self):
+        return self.ref.shape
+
+
+def build_oracle(ref: bool | None = None, quiet=True) -> None:
+    """Compile liboracle.so (and the reference library when the reference
+    tree exists and `ref` is not False)."""
+    targets = ["all"]
+    if ref or (ref is None and os.path.isdir(REFERENCE_TREE)):
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, *targets], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+
+
+_LIBS: dict = {}
+
+
+def _bind(lib: C.CDLL, prefix: str):
+    V, P = C.POINTER(Views), C.POINTER(Config)
+    f = lambda name: getattr(lib, prefix + name)
+    f("compute_ncc").restype = NccResult
+    f("compute_ncc").argtypes = [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int32,
+                                 C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int32]
+    f("evaluate_candidates").argtypes = [V, P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+    f("patchmatch_stereo").restype = C.c_uint32
+    f("patchmatch_stereo").argtypes = [V, P, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_float),
+                                       C.POINTER(C.c_uint8), C.POINTER(C.c_float)]
+    f("refine_subpixel").restype = C.c_uint32
+    f("refine_subpixel").argtypes = [V, P, C.POINTER(C.c_float), C.POINTER(C.c_uint8), C.POINTER(C.c_float)]
+    f("select_source_views").restype = C.c_int32
+    f("select_source_views").argtypes = [C.POINTER(Pose), C.POINTER(Pose), C.c_int32, C.POINTER(Intrinsics), P,
+                                         C.POINTER(C.c_int32)]
+    f("pixel_to_ray").argtypes = [C.POINTER(Intrinsics), C.c_double, C.c_double, C.POINTER(C.c_double)]
+    f("project_point").restype = C.c_int32
+    f("project_point").argtypes = [C.POINTER(Intrinsics), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]
+
+
+def load(which: str = "oracle") -> "Checker":
+    """which = 'oracle' (the C restatement) or 'reference' (the reference's
+    own sources)."""
+    if which in _LIBS:
+        return _LIBS[which]
+    path = ORACLE_SO if which == "oracle" else REF_SO
+    if not os.path.exists(path):
+        build_oracle(ref=(which == "reference"))
+    lib = C.CDLL(path)
+    prefix = "orc_" if which == "oracle" else "ref_"
+    _bind(lib, prefix)
+    if which == "oracle":
+        d = C.POINTER(C.c_double)
+        i32 = C.POINTER(C.c_int32)
+        V, P = C.POINTER(Views), C.POINTER(Config)
+        lib.orc_pm_init.argtypes = [V, P, d, C.c_int32, d, d, i32]
+        lib.orc_pm_sweep.argtypes = [V, P, C.c_int32, C.c_int32, d, d, i32, d, d, i32]
+        lib.orc_pm_output.restype = C.c_uint32
+        lib.orc_pm_output.argtypes = [V, P, d, d, i32, C.POINTER(C.c_float), C.POINTER(C.c_uint8),
+                                      C.POINTER(C.c_float)]
+        lib.orc_pm_prepare.restype = C.c_int32
+        lib.orc_pm_prepare.argtypes = [V, P, d, d, d]
+        lib.orc_refine_pixels.argtypes = [V, P, C.POINTER(C.c_float), C.c_int32, i32, i32, d, d, i32]
+        lib.orc_fuse_depth_maps.restype = C.c_int64
+        lib.orc_fuse_depth_maps.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
+                                            P, C.c_int64, C.POINTER(C.c_int64), d, d, C.POINTER(C.c_float),
+                                            C.POINTER(C.c_uint32)]
+        lib.orc_plane_costs.argtypes = [V, P, C.c_int32, C.c_int32, i32, i32, d, d, d, i32, d]
+        lib.orc_geo_consistency.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
+                                            C.c_int32, C.POINTER(ConsistencyParams), C.POINTER(C.c_uint8),
+                                            C.POINTER(C.c_uint8)]
+        lib.orc_relative_transform_f32.argtypes = [C.POINTER(Pose), C.POINTER(Pose), C.POINTER(C.c_float),
+                                                   C.POINTER(C.c_float)]
+        lib.orc_undistort.argtypes = [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.POINTER(Intrinsics),
+                                      C.POINTER(C.c_float)]
+        lib.orc_xorshift_next.restype = C.c_uint32
+        lib.orc_xorshift_next.argtypes = [C.POINTER(C.c_uint64)]
+        lib.orc_apply_distortion.argtypes = [C.POINTER(Intrinsics), C.c_double, C.c_double, d, d]
+    else:
+        lib.ref_fuse_depth_maps.restype = C.c_int64
+        lib.ref_fuse_depth_maps.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
+                                            C.POINTER(Config), C.c_int64, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_float)]
+    chk = Checker(lib, prefix)
+    _LIBS[which] = chk
+    return chk
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO) or os.path.isdir(REFERENCE_TREE)
+
+
+@dataclass
+class PmOutput:
+    filled: int
+    depth: np.ndarray
+    support: np.ndarray
+    confidence: np.ndarray
+
+
+class Checker:
+    """Python face of one checker library; method names follow the
+    reference functions they restate."""
+
+    def __init__(self, lib, prefix):
+        self.lib = lib
+        self.prefix = prefix
+
+    def _f(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def compute_ncc(self, ref, src, ref_u, ref_v, src_u, src_v, patch_size=11):
+        ref = np.ascontiguousarray(ref, np.uint8)
+        src = np.ascontiguousarray(src, np.uint8)
+        return self._f("compute_ncc")(_ptr(ref, C.c_uint8), ref.shape[1], ref.shape[0], _ptr(src, C.c_uint8),
+                                      src.shape[1], src.shape[0], ref_u, ref_v, src_u, src_v, patch_size)
+
+    def evaluate_candidates(self, vs: ViewSet, cfg: Config, px, py, inv):
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        inv = np.ascontiguousarray(inv, np.float64)
+        cost = np.zeros(len(px), np.float64)
+        vv = np.zeros(len(px), np.int32)
+        self._f("evaluate_candidates")(C.byref(vs.struct), C.byref(cfg), len(px), _ptr(px, C.c_int32),
+                                       _ptr(py, C.c_int32), _ptr(inv, C.c_double), _ptr(cost, C.c_double),
+                                       _ptr(vv, C.c_int32))
+        return cost, vv
+
+    def patchmatch_stereo(self, vs: ViewSet, cfg: Config, seeds=None) -> PmOutput:
+        h, w = vs.shape
+        depth = np.full((h, w), np.nan, np.float32)
+        sup = np.zeros((h, w), np.uint8)
+        conf = np.zeros((h, w), np.float32)
+        if seeds is not None and len(seeds):
+            s = np.ascontiguousarray(seeds, np.float64).reshape(-1, 3)
+            sp, ns = _ptr(s, C.c_double), len(s)
+        else:
+            sp, ns = None, 0
+        filled = self._f("patchmatch_stereo")(C.byref(vs.struct), C.byref(cfg), sp, ns, _ptr(depth, C.c_float),
+                                              _ptr(sup, C.c_uint8), _ptr(conf, C.c_float))
+        return PmOutput(int(filled), depth, sup, conf)
+
+    def refine_subpixel(self, vs: ViewSet, cfg: Config, pm: PmOutput) -> PmOutput:
+        depth = pm.depth.copy()
+        sup = pm.support.copy()
+        conf = pm.confidence.copy()
+        n = self._f("refine_subpixel")(C.byref(vs.struct), C.byref(cfg), _ptr(depth, C.c_float),
+                                       _ptr(sup, C.c_uint8), _ptr(conf, C.c_float))
+        return PmOutput(int(n), depth, sup, conf)
+
+    def select_source_views(self, ref_pose, poses, intr, cfg: Config):
+        ps = (Pose * len(poses))(*[pose_from(p) for p in poses])
+        out = np.zeros(max(1, len(poses)), np.int32)
+        rp = pose_from(ref_pose)
+        k = intrinsics_from(intr)
+        n = self._f("select_source_views")(C.byref(rp), C.cast(ps, C.POINTER(Pose)), len(poses), C.byref(k),
+                                           C.byref(cfg), _ptr(out, C.c_int32))
+        return out[:n].tolist()
+
+    def pixel_to_ray(self, intr, u, v):
+        k = intrinsics_from(intr)
+        ray = np.zeros(3, np.float64)
+        self._f("pixel_to_ray")(C.byref(k), u, v, _ptr(ray, C.c_double))
+        return ray
+
+    def project_point(self, intr, p):
+        k = intrinsics_from(intr)
+        p = np.ascontiguousarray(p, np.float64)
+        u, v = C.c_double(), C.c_double()
+        ok = self._f("project_point")(C.byref(k), _ptr(p, C.c_double), C.byref(u), C.byref(v))
+        return bool(ok), u.value, v.value
+
+    # ---- restatement-only entry points ----
+    def pm_init(self, vs: ViewSet, cfg: Config, seeds=None):
+        h, w = vs.shape
+        inv = np.zeros(h * w, np.float64)
+        cost = np.zeros(h * w, np.float64)
+        sup = np.zeros(h * w, np.int32)
+        if seeds is not None and len(seeds):
+            s = np.ascontiguousarray(seeds, np.float64).reshape(-1, 3)
+            sp, ns = _ptr(s, C.c_double), len(s)
+        else:
+            sp, ns = None, 0
+        self.lib.orc_pm_init(C.byref(vs.struct), C.byref(cfg), sp, ns, _ptr(inv, C.c_double),
+                             _ptr(cost, C.c_double), _ptr(sup, C.c_int32))
+        return inv, cost, sup
+
+    def pm_sweep(self, vs: ViewSet, cfg: Config, it, direction, inv, cost, sup):
+        inv = np.ascontiguousarray(inv, np.float64)
+        cost = np.ascontiguousarray(cost, np.float64)
+        sup = np.ascontiguousarray(sup, np.int32)
+        oi, oc, os_ = np.empty_like(inv), np.empty_like(cost), np.empty_like(sup)
+        self.lib.orc_pm_sweep(C.byref(vs.struct), C.byref(cfg), it, direction, _ptr(inv, C.c_double),
+                              _ptr(cost, C.c_double), _ptr(sup, C.c_int32), _ptr(oi, C.c_double),
+                              _ptr(oc, C.c_double), _ptr(os_, C.c_int32))
+        return oi, oc, os_
+
+    def pm_prepare(self, vs: ViewSet, cfg: Config):
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        ok = self.lib.orc_pm_prepare(C.byref(vs.struct), C.byref(cfg), C.byref(a), C.byref(b), C.byref(c))
+        return bool(ok), a.value, b.value, c.value
+
+    def refine_pixels(self, vs: ViewSet, cfg: Config, depth, px, py):
+        depth = np.ascontiguousarray(depth, np.float32)
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        bi = np.zeros(len(px), np.float64)
+        bc = np.zeros(len(px), np.float64)
+        wr = np.zeros(len(px), np.int32)
+        self.lib.orc_refine_pixels(C.byref(vs.struct), C.byref(cfg), _ptr(depth, C.c_float), len(px),
+                                   _ptr(px, C.c_int32), _ptr(py, C.c_int32), _ptr(bi, C.c_double),
+                                   _ptr(bc, C.c_double), _ptr(wr, C.c_int32))
+        return bi, bc, wr
+
+    def plane_costs(self, vs: ViewSet, cfg: Config, best_k, px, py, inv, normals):
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        inv = np.ascontiguousarray(inv, np.float64)
+        nrm = np.ascontiguousarray(normals, np.float64).reshape(-1, 3)
+        n = len(px)
+        cost = np.zeros(n, np.float64)
+        vv = np.zeros(n, np.int32)
+        view_cost = np.zeros((n, len(vs.srcs)), np.float64)
+        self.lib.orc_plane_costs(C.byref(vs.struct), C.byref(cfg), best_k, n, _ptr(px, C.c_int32),
+                                 _ptr(py, C.c_int32), _ptr(inv, C.c_double), _ptr(nrm, C.c_double),
+                                 _ptr(cost, C.c_double), _ptr(vv, C.c_int32), _ptr(view_cost, C.c_double))
+        return cost, vv, view_cost
+
+    def undistort(self, img, intr):
+        img = np.ascontiguousarray(img, np.uint8)
+        out = np.zeros(img.shape, np.float32)
+        k = intrinsics_from(intr)
+        self.lib.orc_undistort(_ptr(img, C.c_uint8), img.shape[1], img.shape[0], C.byref(k), _ptr(out, C.c_float))
+        return out
+
+
+def depth_maps_struct(maps):
+    """maps: list of (depth float32 HxW, support uint8, confidence float32)."""
+    keep = []
+    arr = (DepthMapC * len(maps))()
+    for i, (d, s, c) in enumerate(maps):
+        d = np.ascontiguousarray(d, np.float32)
+        s = np.ascontiguousarray(s, np.uint8)
+        c = np.ascontiguousarray(c, np.float32)
+        keep += [d, s, c]
+        arr[i] = DepthMapC(d.shape[1], d.shape[0], _ptr(d, C.c_float), _ptr(s, C.c_uint8), _ptr(c, C.c_float))
+    return arr, keep
+
+
+def fuse_depth_maps(which: str, maps, poses, intrinsics, cfg: Config):
+    """Returns positions (N,3), normals (N,3), confidences (N,), sorted
+    lexicographically by position (the reference emits unordered_map
+    order)."""
+    chk = load(which)
+    arr, keep = depth_maps_struct(maps)
+    ps = (Pose * len(poses))(*[pose_from(p) for p in poses])
+    ks = (Intrinsics * len(intrinsics))(*[intrinsics_from(k) for k in intrinsics])
+    cap = int(sum(m[0].size for m in maps)) + 1
+    pos = np.zeros((cap, 3), np.float64)
+    nrm = np.zeros((cap, 3), np.float64)
+    conf = np.zeros(cap, np.float32)
+    if which == "oracle":
+        keys = np.zeros(cap, np.int64)
+        cnt = np.zeros(cap, np.uint32)
+        n = chk.lib.orc_fuse_depth_maps(arr, len(maps), C.cast(ps, C.POINTER(Pose)), C.cast(ks, C.POINTER(Intrinsics)),
+                                        C.byref(cfg), cap, _ptr(keys, C.c_int64), _ptr(pos, C.c_double),
+                                        _ptr(nrm, C.c_double), _ptr(conf, C.c_float), _ptr(cnt, C.c_uint32))
+    else:
+        n = chk.lib.ref_fuse_depth_maps(arr, len(maps), C.cast(ps, C.POINTER(Pose)), C.cast(ks, C.POINTER(Intrinsics)),
+                                        C.byref(cfg), cap, _ptr(pos, C.c_double), _ptr(nrm, C.c_double),
+                                        _ptr(conf, C.c_float))
+    del keep
+    pos, nrm, conf = pos[:n], nrm[:n], conf[:n]
+    order = np.lexsort((pos[:, 2], pos[:, 1], pos[:, 0]))
+    return pos[order], nrm[order], conf[order]
+
+
+def geo_consistency(maps, poses, intrinsics, ref_index, rel_depth_max, reproj_px_max, min_views):
+    chk = load("oracle")
+    arr, keep = depth_maps_struct(maps)
+    ps = (Pose * len(poses))(*[pose_from(p) for p in poses])
+    ks = (Intrinsics * len(intrinsics))(*[intrinsics_from(k) for k in intrinsics])
+    prm = ConsistencyParams(rel_depth_max, reproj_px_max, min_views)
+    h, w = maps[ref_index][0].shape
+    cnt = np.zeros((h, w), np.uint8)
+    kp = np.zeros((h, w), np.uint8)
+    chk.lib.orc_geo_consistency(arr, len(maps), C.cast(ps, C.POINTER(Pose)), C.cast(ks, C.POINTER(Intrinsics)),
+                                ref_index, C.byref(prm), _ptr(cnt, C.c_uint8), _ptr(kp, C.c_uint8))
+    del keep
+    return cnt, kp
+
+
+def config_fields():
+    return [f[0] for f in _CONFIG_FIELDS]
+
+
+__all__ = ["load", "make_config", "ViewSet", "Config", "CONFIG_DEFAULTS", "fuse_depth_maps",
+           "geo_consistency", "reference_available", "build_oracle", "fields"]
