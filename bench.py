@@ -1,0 +1,382 @@
+"""Benchmark: depth maps/s of plane-mode PatchMatch MVS on one GB300.
+
+Workload (the headline configuration): one reference view + 8 sources at
+1920x1440, f = 1450 px with Brown-Conrady distortion (k1 = 0.05,
+k2 = -0.01), the tabletop scene (sphere, box, three cylinders on a tilted
+plane, value-noise albedo with 10 % weak-texture patches), 11x11 windows,
+8 iterations, FP32.  A step = one depth map: initialisation, 8 red-black
+iterations, sub-pixel refinement, output.  Images are undistorted on the
+device when staged.
+
+  value  -- depth maps/s with the staged inputs resident in HBM; each step
+            is timed with CUDA events on the engine's stream and L2 is
+            flushed (a 512 MiB write) between steps, outside the events;
+  e2e    -- the same metric through the public C ABI from host buffers:
+            stage (H2D of 9 8-bit images + undistortion + textures),
+            run, download (depth, support, confidence, normal, cost), release.
+
+`--impl reference` times the reference algorithm on the host cores instead
+(the CPU oracle restatement of patchmatch_stereo.cpp, all threads) on a
+bounded sample of the same workload, extrapolated to one depth map.
+
+Multi-GPU: the path does not shard (replicas only); each rank runs its own
+replica and value = total depth maps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "recon-scanner_gb300"))
+
+METRIC = "depth maps/s 1920×1440×8src (1 GB300), chosen vs plain GPU at ≤0.1% depth err"
+K, S_SRC = 11, 8
+W, H, F, ITERS = 1920, 1440, 1450.0, 8
+# per pixel-hypothesis algorithmic FLOP, plane-induced homography mode:
+# S * (K^2 * 26 + 30) + 40  (26 = 15 projection + 6 bilinear + 5 moments)
+FLOP_PER_HYP = S_SRC * (K * K * 26 + 30) + 40
+SM_COUNT, FP32_LANES = 152, 128
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_scene(device):
+    import synthetic as Syn
+
+    return Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device)
+
+
+def views_of(M, sc):
+    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    return M.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+
+
+def config_of(M, sc):
+    return M.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=ITERS, patch_size=K,
+                       subpixel_iterations=4)
+
+
+def dist_init():
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not dist.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm / baseline
+# ---------------------------------------------------------------------------
+
+def cpu_reference_sample(sc, cols=480, refine_rows=4, threads=None):
+    """Time the reference algorithm (the oracle's restatement of
+    patchmatch_stereo.cpp) on a crop of the workload and extrapolate to one
+    depth map.  The crop is 16 x threads rows tall -- the reference splits
+    its sweeps into min(threads, H/16) row blocks, so this keeps every
+    thread busy -- and `cols` wide, centred.  PatchMatch: initial cost + one
+    iteration (4 direction sweeps), scaled to ITERS iterations and the full
+    frame; RefineSubpixel (single-threaded in the reference) on
+    `refine_rows` rows, scaled to the frame.
+    Returns (seconds per depth map, threads, note)."""
+    import copy
+
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build_oracle(ref=False)
+    orc = O.load("oracle")
+    threads = threads or os.cpu_count() or 1
+    rows = min(H, 16 * threads)
+    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+    und = [c.undistorted() for c in cams]
+    imgs = [np.clip(np.round(orc.undistort(im, c.intrinsics_array())), 0, 255).astype(np.uint8)
+            for im, c in zip([sc.ref.image] + [s.image for s in sc.sources], cams)]
+    x0 = W // 2 - cols // 2
+
+    def crop(nrows):
+        y0 = H // 2 - nrows // 2
+        cr = copy.deepcopy(und[0])
+        cr.cx, cr.cy = und[0].cx - x0, und[0].cy - y0
+        cr.width, cr.height = cols, nrows
+        ref = np.ascontiguousarray(imgs[0][y0:y0 + nrows, x0:x0 + cols])
+        return O.ViewSet(ref, imgs[1:], cr, und[1:])
+
+    def cfg(iters):
+        return O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=iters, patch_size=K,
+                             num_threads=threads, subpixel_iterations=4)
+
+    vs = crop(rows)
+    t0 = time.perf_counter()
+    orc.patchmatch_stereo(vs, cfg(0))
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pm = orc.patchmatch_stereo(vs, cfg(1))
+    t_one = max(0.0, time.perf_counter() - t0 - t_init)
+    vs_r = crop(refine_rows)
+    r0 = rows // 2 - refine_rows // 2
+    pm_r = type(pm)(pm.filled, np.ascontiguousarray(pm.depth[r0:r0 + refine_rows]),
+                    np.ascontiguousarray(pm.support[r0:r0 + refine_rows]),
+                    np.ascontiguousarray(pm.confidence[r0:r0 + refine_rows]))
+    t0 = time.perf_counter()
+    orc.refine_subpixel(vs_r, cfg(1), pm_r)
+    t_ref = time.perf_counter() - t0
+    area = (W * H) / (cols * rows)
+    total = (t_init + ITERS * t_one) * area + t_ref * (W * H) / (cols * refine_rows)
+    note = (f"reference algorithm (oracle restatement of patchmatch_stereo.cpp), {threads} threads: initial cost + "
+            f"1 iteration on a centred {cols}x{rows} crop, scaled x{ITERS} iterations and x{area:.1f} to the frame; "
+            f"single-threaded RefineSubpixel on {cols}x{refine_rows}, scaled to the frame; "
+            f"{t_init + t_one + t_ref:.1f} s measured")
+    return total, threads, note
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    sc = make_scene("cpu")
+    secs = []
+    threads = os.cpu_count() or 1
+    note = ""
+    for i in range(args.warmup + args.steps):
+        t, threads, note = cpu_reference_sample(sc)
+        if i >= args.warmup:
+            secs.append(t)
+    per_map = statistics.mean(secs)
+    value = 1.0 / per_map
+    line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_map * 1000.0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tabletop scene, analytic truth)",
+            "impl": "reference",
+            "config": {"workload": f"tabletop {W}x{H}, {S_SRC} sources, {K}x{K}, {ITERS} iterations",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "depth maps/s", "cores": threads, "kind": "port",
+                             "sample": note},
+            "e2e": {"value": value, "unit": "depth maps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    import recon_mvs as M
+
+    M.load_library()
+    peaks, peak_src = load_peaks()
+    sc = make_scene(f"cuda:{local}")
+    views = views_of(M, sc)
+    cfg = config_of(M, sc)
+    opts = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if args.fp16 else M.STORAGE_FP32,
+                     device=local, refine=1)
+    eng = M.Engine(opts)
+    job = eng.stage(views, cfg, undistort=True)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        eng.run(job)
+        eng.synchronize()
+
+    # ---- resident: per-step CUDA-event time on the engine's stream ----
+    step_ms, sweep_ms, hyps = [], [], []
+    launches_per_step = 0
+    barrier(world)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.random_(0, 255)  # L2 flush, outside the timed events
+            torch.cuda.synchronize()
+            h0 = eng.stats().hypotheses_evaluated
+            eng.run(job)
+            eng.synchronize()
+            st = eng.stats()
+            step_ms.append(st.last_run_ms)
+            sweep_ms.append(st.last_sweep_ms)
+            hyps.append(st.hypotheses_evaluated - h0)
+            launches_per_step = st.last_sweep_launches + 3  # init, refine, output
+    barrier(world)
+    total_ms = barrier_max(world, float(sum(step_ms)))
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # ---- end to end through the C ABI from host buffers ----
+    dm = M.DepthMap.allocate(W, H)
+    e2e_times = []
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        j = eng.stage(views, cfg, undistort=True)
+        eng.run(j)
+        eng.download(j, dm)
+        eng.release(j)
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_times.append(t1 - t0)
+    e2e_s = barrier_max(world, statistics.mean(e2e_times))
+    e2e_value = world / e2e_s
+    h2d = (1 + S_SRC) * W * H
+    d2h = W * H * (4 + 1 + 4 + 12 + 4) + 4
+
+    # ---- roofline of the dominant kernel (the red-black sweep) ----
+    sweeps = launches_per_step - 3
+    per_launch_ms = statistics.mean(sweep_ms) / max(1, sweeps)
+    hyp_per_launch = statistics.mean(hyps) / max(1, sweeps)
+    achieved_tflops = FLOP_PER_HYP * hyp_per_launch / (per_launch_ms * 1e-3) / 1e12
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    peak_tflops = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("plane_sweep_bytes_per_launch_full")
+
+    # accuracy of this map vs analytic truth (reported, not timed)
+    err = np.abs(dm.depth.astype(np.float64) - sc.ref.depth)
+    rel = err / sc.ref.depth
+    ok = np.isfinite(rel)
+    acc = {"filled": float(np.isfinite(dm.depth).mean()),
+           "median_rel_err": float(np.median(rel[ok])) if ok.any() else None,
+           "p95_rel_err": float(np.quantile(rel[ok], 0.95)) if ok.any() else None,
+           "median_abs_err_mm": float(np.median(err[ok]) * 1e3) if ok.any() else None}
+
+    line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp16-storage/f32" if args.fp16 else "f32",
+            "data": "synthetic (seeded tabletop scene, analytic truth)",
+            "config": {"workload": f"tabletop {W}x{H}, {S_SRC} sources, {K}x{K}, {ITERS} iterations, "
+                                   f"plane mode, best_k={args.best_k}, golden-section refine",
+                       "storage": "fp16" if args.fp16 else "fp32",
+                       "l2": "flushed between steps (512 MiB write, outside the timed events)",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches_per_step * args.steps,
+            "e2e": {"value": e2e_value, "unit": "depth maps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / peak_tflops, "traffic": traffic,
+                         "kernel": "k_plane_sweep",
+                         "peak_source": f"{SM_COUNT} SMs x {FP32_LANES} FP32 lanes x 2 x sm_max_mhz {sm_mhz} "
+                                        f"({peak_src} MEASURED_PEAKS.json clock)",
+                         "hypotheses_per_launch": hyp_per_launch, "ms_per_launch": per_launch_ms,
+                         "flop_per_hypothesis": FLOP_PER_HYP},
+            "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
+            "accuracy": acc, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        secs, threads, note = cpu_reference_sample(sc)
+        line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
+                                "sample": note}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--best-k", type=int, default=4)
+    ap.add_argument("--fp16", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

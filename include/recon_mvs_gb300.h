@@ -1,0 +1,314 @@
+/*
+ * recon_mvs_gb300.h -- C ABI of the GB300 PatchMatch multi-view-stereo
+ * engine (librecon_mvs_gb300.so).
+ *
+ * A drop-in for the MVS path of kai3934908500/recon-scanner:
+ *   core/include/recon/mvs.h:133-214 (SelectSourceViews, ComputeNcc,
+ *   PatchMatchStereo, RefineSubpixel, FuseDepthMaps) and the conventions of
+ *   core/include/recon/recon_c_api.h (POD structs, recon_status returns, no
+ *   exception crosses the boundary, core-allocated buffers freed by the
+ *   library).  Every entry point below names the reference interface it
+ *   replaces.
+ *
+ * Memory: unless stated otherwise every pointer is HOST memory owned by the
+ * caller and only read/written during the call.  Images are tightly packed
+ * 8-bit grayscale (stride = width), as in the reference.
+ *
+ * Threading: one context per host thread; the stateless entry points use a
+ * per-thread default context on the options' device.
+ *
+ * When recon_c_api.h is used as well, include it first: the shared types
+ * (recon_camera_intrinsics, recon_pose, recon_status) are then taken from it.
+ */
+#ifndef RECON_MVS_GB300_H_
+#define RECON_MVS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RECON_MVS_GB300_ABI_VERSION 1
+
+/* recon_c_api.h:31-37 */
+#ifndef RECON_API
+#if defined(__GNUC__) || defined(__clang__)
+#define RECON_API __attribute__((visibility("default")))
+#else
+#define RECON_API
+#endif
+#endif
+
+#ifndef RECON_RECON_C_API_H_
+/* Same layout as recon_camera_intrinsics (recon_c_api.h:44-56). */
+typedef struct recon_camera_intrinsics {
+  double fx, fy, cx, cy;
+  double k1, k2, k3, p1, p2;
+  double width, height;
+} recon_camera_intrinsics;
+
+/* Same layout as recon_pose (recon_c_api.h:59-63): world -> camera,
+ * r row-major, t in metres. */
+typedef struct recon_pose {
+  double r[9];
+  double t[3];
+  double timestamp_ns;
+} recon_pose;
+
+/* The subset of recon_status (recon_c_api.h:135-207) this engine returns,
+ * with the reference's numeric values. */
+typedef enum recon_status {
+  RECON_OK = 0,
+  RECON_ERR_INVALID_ARGUMENT = 1,
+  RECON_ERR_OUT_OF_MEMORY = 2,
+  RECON_ERR_NOT_IMPLEMENTED = 3,
+  RECON_ERR_INTERNAL = 4,
+  RECON_ERR_CANCELLED = 5,
+  RECON_ERR_MVS_NO_DEPTH = 500,
+  RECON_ERR_MVS_FILTER_EXHAUSTED = 501,
+  RECON_ERR_MVS_GPU_FAILURE = 502
+} recon_status;
+#endif
+
+/* recon::MvsConfig (core/include/recon/mvs.h:24-67), field for field and in
+ * order; bool fields are int32.  recon_mvs_config_default() gives the
+ * reference defaults. */
+typedef struct recon_mvs_config {
+  int32_t num_views;
+  int32_t ref_view_index;
+  double ideal_angle_min_deg;
+  double ideal_angle_max_deg;
+  double max_view_scale_mismatch;
+  double view_angle_weight;
+  double view_texture_weight;
+  double view_spread_weight;
+  double view_scale_weight;
+  double reference_depth_m;
+  int32_t patch_size;
+  int32_t iterations;
+  int32_t random_search_count;
+  double random_search_radius_ratio;
+  double restart_ratio;
+  int32_t propagation_directions;
+  int32_t propagation_enabled;
+  int32_t num_threads;
+  double photo_threshold;
+  double depth_regularization;
+  double geo_consistency_threshold;
+  double weak_texture_variance;
+  int32_t subpixel_iterations;
+  int32_t subpixel_fit_points;
+  double subpixel_window_ratio;
+  double min_depth_m;
+  double max_depth_m;
+  int32_t min_view_consistency;
+  double fusion_voxel_size_m;
+} recon_mvs_config;
+
+/* Search model. */
+typedef enum recon_mvs_mode {
+  /* The reference algorithm (patchmatch_stereo.cpp:422-764): fronto-parallel
+   * inverse-depth hypotheses, translated NCC windows, mean NCC over valid
+   * views, its Jacobi direction sweeps and row-block xorshift draws.  Depth
+   * maps match the reference's up to FP32-vs-FP64 cost rounding; results
+   * depend on num_threads exactly as the reference's do. */
+  RECON_MVS_MODE_COMPAT = 0,
+  /* The GB300 engine: plane hypotheses (inverse depth + normal), per-sample
+   * homography windows, mean of the best_k view costs, red-black
+   * checkerboard propagation with adaptive neighbour selection and random
+   * perturbation.  Requires undistorted (pinhole) images. */
+  RECON_MVS_MODE_PLANE = 1
+} recon_mvs_mode;
+
+typedef enum recon_mvs_storage {
+  RECON_MVS_STORAGE_FP32 = 0, /* source images as FP32 textures */
+  RECON_MVS_STORAGE_FP16 = 1  /* FP16 textures: exact for 8-bit input */
+} recon_mvs_storage;
+
+typedef struct recon_mvs_options {
+  int32_t mode;       /* recon_mvs_mode */
+  int32_t storage;    /* recon_mvs_storage */
+  int32_t best_k;     /* plane mode: views averaged per hypothesis, <= 8; 0 = all valid */
+  int32_t refine;     /* plane mode: 1 = golden-section inverse-depth refinement after the sweeps */
+  uint64_t seed;      /* plane mode random stream */
+  int32_t device;     /* CUDA device ordinal */
+  int32_t reserved[7];
+} recon_mvs_options;
+
+/* Inputs of one reference view: the PatchMatchStereo argument list
+ * (mvs.h:164-177) with its index contract (mvs.h:151-161): src_gray /
+ * src_w / src_h use the relative index k; poses the global index
+ * source_indices[k]; src_intrinsics are global when num_src_intrinsics ==
+ * num_src_poses, else relative when == num_src. */
+typedef struct recon_mvs_views {
+  const uint8_t* ref_gray;
+  int32_t ref_w, ref_h;
+  int32_t num_src;
+  const uint8_t* const* src_gray;
+  const int32_t* src_w;
+  const int32_t* src_h;
+  const recon_pose* ref_pose;
+  const recon_pose* src_poses;
+  int32_t num_src_poses;
+  const recon_camera_intrinsics* ref_intr;
+  const recon_camera_intrinsics* src_intrinsics;
+  int32_t num_src_intrinsics;
+  const int32_t* source_indices;
+} recon_mvs_views;
+
+/* recon::DepthMap (mvs.h:85-109), caller-allocated width*height arrays.
+ * depth NaN = invalid.  normal (3 floats per pixel, reference camera
+ * frame) and cost are optional outputs (NULL = not wanted). */
+typedef struct recon_mvs_depth_map {
+  int32_t width, height;
+  float* depth;
+  uint8_t* support_count;
+  float* confidence;
+  float* normal;
+  float* cost;
+} recon_mvs_depth_map;
+
+/* recon::NccResult (mvs.h:70-75). */
+typedef struct recon_mvs_ncc_result {
+  int32_t valid;
+  double ncc;
+  int32_t weak_texture;
+  int32_t valid_samples;
+} recon_mvs_ncc_result;
+
+/* recon::PointCloud (mvs.h:112-125), library-allocated; release with
+ * recon_mvs_point_cloud_free.  keys / counts are the voxel key of each
+ * point and the number of pixels fused into it. */
+typedef struct recon_mvs_point_cloud {
+  int64_t count;
+  double* positions;
+  double* normals;
+  float* colors;
+  float* confidences;
+  int64_t* keys;
+  uint32_t* counts;
+} recon_mvs_point_cloud;
+
+typedef struct recon_mvs_stats {
+  uint64_t hypotheses_evaluated; /* plane sweeps: hypotheses whose windows were evaluated */
+  double last_run_ms;            /* device time of the last PatchMatch run (CUDA events) */
+  double last_sweep_ms;          /* device time of its sweeps only */
+  int32_t last_sweep_launches;
+  int32_t reserved[5];
+} recon_mvs_stats;
+
+/* ---- version and configuration ---------------------------------------- */
+
+/* recon_abi_version (recon_c_api.h:430) */
+RECON_API uint32_t recon_mvs_abi_version(void);
+/* MvsConfig{} defaults (mvs.h:24-67) */
+RECON_API void recon_mvs_config_default(recon_mvs_config* cfg);
+RECON_API void recon_mvs_options_default(recon_mvs_options* opts);
+/* recon_set_param (c_api.cpp:158-180) + ParamStore::Set clamping
+ * (params.cpp:133-157) for the 15 mvs_* keys (params.h:162-177), mapped
+ * onto MvsConfig as Orchestrator::StageMvs does (orchestrator.cpp:952-970).
+ * Unknown keys: RECON_ERR_INVALID_ARGUMENT. */
+RECON_API recon_status recon_mvs_config_set_param(recon_mvs_config* cfg, const char* key, int32_t value_int,
+                                                  double value_double);
+/* recon_apply_preset (recon_c_api.h:442): 0 fast, 1 standard, 2 high. */
+RECON_API recon_status recon_mvs_config_apply_preset(recon_mvs_config* cfg, int32_t preset);
+
+/* ---- the MVS functions --------------------------------------------------- */
+
+/* recon::SelectSourceViews (mvs.h:133-136; patchmatch_stereo.cpp:133-211).
+ * Host-side geometry; writes up to `capacity` global indices. */
+RECON_API recon_status recon_mvs_select_source_views(const recon_pose* ref_pose, const recon_pose* poses,
+                                                     int32_t num_poses, const recon_camera_intrinsics* intr,
+                                                     const recon_mvs_config* cfg, int32_t* out_indices,
+                                                     int32_t capacity, int32_t* out_count);
+
+/* recon::ComputeNcc (mvs.h:144-146; patchmatch_stereo.cpp:214-274) for n
+ * windows (coords: n x {ref_u, ref_v, src_u, src_v}); FP64 on the GPU,
+ * bit-identical to the reference. */
+RECON_API recon_status recon_mvs_compute_ncc(const uint8_t* ref, int32_t ref_w, int32_t ref_h, const uint8_t* src,
+                                             int32_t src_w, int32_t src_h, const double* coords, int32_t n,
+                                             int32_t patch_size, recon_mvs_ncc_result* out);
+
+/* Cost of n given hypotheses at integer pixels (px, py): the
+ * EvaluateCandidate of patchmatch_stereo.cpp:344-418 in COMPAT mode
+ * (inv_depth only), the plane cost in PLANE mode (inv_depth + normals,
+ * 3 floats each).  out_view_cost (n x num_src, optional) holds 1 - NCC per
+ * view, 1e30 for invalid views. */
+RECON_API recon_status recon_mvs_evaluate(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                          const recon_mvs_options* opts, int32_t n, const int32_t* px,
+                                          const int32_t* py, const double* inv_depth, const float* normals,
+                                          float* out_cost, int32_t* out_support, float* out_view_cost);
+
+/* recon::PatchMatchStereo (mvs.h:164-177).  seed_points: num_seeds x
+ * {u, v, depth_m} or NULL.  Contract violations (mvs.h:151-161) return
+ * RECON_ERR_INVALID_ARGUMENT and leave `out` untouched, where the reference
+ * returns 0; a degenerate baseline or depth range returns RECON_OK with
+ * *out_filled = 0 and an all-invalid map, as the reference does. */
+RECON_API recon_status recon_mvs_patchmatch(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                            const recon_mvs_options* opts, const double* seed_points,
+                                            int32_t num_seeds, recon_mvs_depth_map* out, uint32_t* out_filled);
+
+/* recon::RefineSubpixel (mvs.h:185-196; patchmatch_stereo.cpp:770-979):
+ * the reference's 5-point parabola + golden-section refinement of every
+ * valid pixel, in place. */
+RECON_API recon_status recon_mvs_refine_subpixel(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                                 const recon_mvs_options* opts, recon_mvs_depth_map* depth,
+                                                 uint32_t* out_refined);
+
+/* Multi-view geometric consistency of map `ref_index` against the others
+ * (spec: shaders/vulkan/recon_mvs_consistency.comp:94-140 with the strict
+ * transform of shaders/common/gpu_algo.h:537-538, plus a reprojection
+ * bound).  out_count: consistent maps per pixel; out_keep: count >=
+ * min_views (both width*height of the reference map). */
+RECON_API recon_status recon_mvs_geometric_consistency(const recon_mvs_depth_map* maps, const recon_pose* poses,
+                                                       const recon_camera_intrinsics* intr, int32_t num_maps,
+                                                       int32_t ref_index, float rel_depth_max, float reproj_px_max,
+                                                       int32_t min_views, uint8_t* out_count, uint8_t* out_keep);
+
+/* recon::FuseDepthMaps (mvs.h:203-206; patchmatch_stereo.cpp:985-1089).
+ * keep_masks (optional, one per map, may contain NULLs) drop pixels before
+ * fusion (the geometric-consistency filter).  The cloud is bit-identical to
+ * the reference's; points come in order of the first pixel of each voxel. */
+RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const recon_pose* poses,
+                                      const recon_camera_intrinsics* intr, int32_t num_maps,
+                                      const recon_mvs_config* cfg, const uint8_t* const* keep_masks,
+                                      recon_mvs_point_cloud* out);
+/* recon_free_buffer (recon_c_api.h:435-436) for point clouds. */
+RECON_API void recon_mvs_point_cloud_free(recon_mvs_point_cloud* cloud);
+
+/* Undistortion remap of an 8-bit image to the pinhole camera with the same
+ * fx, fy, cx, cy (inverse map through ApplyDistortion, camera.cpp:33-45);
+ * out: width*height floats, 0 outside the source. */
+RECON_API recon_status recon_mvs_undistort(const uint8_t* img, int32_t w, int32_t h,
+                                           const recon_camera_intrinsics* intr, float* out);
+
+/* ---- device-resident jobs (batching and measurement) --------------------- */
+
+/* A context owns a CUDA stream, device workspaces and staged jobs. */
+RECON_API recon_status recon_mvs_context_create(const recon_mvs_options* opts, void** out_ctx);
+RECON_API void recon_mvs_context_destroy(void* ctx);
+/* Upload and prepare one reference view (images to textures, camera
+ * tables); the job keeps the device copies until released.  When
+ * undistort != 0 the images are first remapped to the pinhole camera
+ * (recon_mvs_undistort) on the device. */
+RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                           int32_t undistort, int32_t* out_job);
+/* Run PatchMatch (+ refinement per options) on staged jobs, asynchronously
+ * on the context's stream. */
+RECON_API recon_status recon_mvs_job_run(void* ctx, int32_t job);
+RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_t n);
+/* Copy a finished job's map to the host (synchronises). */
+RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out,
+                                              uint32_t* out_filled);
+RECON_API recon_status recon_mvs_job_release(void* ctx, int32_t job);
+RECON_API recon_status recon_mvs_synchronize(void* ctx);
+RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out);
+/* Human-readable description of the last error on this thread. */
+RECON_API const char* recon_mvs_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RECON_MVS_GB300_H_ */

@@ -1,0 +1,351 @@
+// cost.cuh -- NCC window cost of one hypothesis against one source view.
+//
+// Two window models share the same NCC rules (patchmatch_stereo.cpp:214-274):
+// a sample counts when both its reference and source positions are inside
+// the image (SampleBilinear's rule, :78-86); fewer than K*K/2 valid samples
+// or sqrt(var_r * var_s) < 1e-9 make the view invalid; NCC is clamped to
+// [-1, 1].
+//
+//  * COMPAT -- the reference's own model (EvaluateCandidate, :344-418): a
+//    fronto-parallel hypothesis; only the window centre is projected; the
+//    source window is the reference window translated to the projected
+//    centre; both images are read with index == coordinate, so the
+//    reference window at pixel centres is the 2x2 box filter of the image.
+//  * PLANE -- a plane hypothesis (inverse depth at the pixel centre + unit
+//    normal): every sample (x+dx+0.5, y+dy+0.5) of the reference window is
+//    mapped through the plane-induced homography into the source and read
+//    with the pixel-centre convention (index == coordinate - 0.5).
+//
+// Per sample the PLANE path costs ~22 FP32 instructions, one MUFU.RCP, one
+// texture gather (the 2x2 bilinear footprint) and one reference read;
+// the window centre is computed once per (hypothesis, view) in float-float.
+// Moments are accumulated on data centred per window (reference window mean,
+// source centre sample) with per-row partial sums, which keeps FP32 NCC
+// within ~1e-6 of an FP64 evaluation.
+#pragma once
+
+#include "common.cuh"
+
+namespace rmvs {
+
+struct ViewResult {
+  float ncc;
+  int valid;
+};
+
+// Window moments of the reference image for one pixel (full window).
+struct RefWindow {
+  float mean;   // mean of (I - 128) over the window (the centring offset)
+  float sxx;    // sum of squared centred values
+  bool full;    // the whole K x K window lies inside the reference image
+};
+
+// Centre of the source window in float-float.  Xn = P + rho * b is the
+// source-camera point scaled by rho (P = A * ray, computed once per pixel in
+// FP64).  Returns false when the point is not in front of the camera
+// (p_src.z <= 1e-6, patchmatch_stereo.cpp:391).
+__device__ __forceinline__ bool source_centre(const SrcView& S, const ff P[3], ff rho, float rho_f, ff* u0,
+                                              ff* v0, float* xz, float* mx, float* my) {
+  const ff Xx = ff_add(P[0], ff_mul(S.bff[0], rho));
+  const ff Xy = ff_add(P[1], ff_mul(S.bff[1], rho));
+  const ff Xz = ff_add(P[2], ff_mul(S.bff[2], rho));
+  // p_src.z = Xz / rho
+  if (!(Xz.hi + Xz.lo > 1e-6f * rho_f)) return false;
+  ff x = ff_div(Xx, Xz);
+  ff y = ff_div(Xy, Xz);
+  *xz = Xz.hi;
+  *mx = x.hi;
+  *my = y.hi;
+  if (S.distorted) {
+    // ApplyDistortion (camera.cpp:33-45) in float-float
+    const ff x2 = ff_mul(x, x), y2 = ff_mul(y, y);
+    const ff r2 = ff_add(x2, y2);
+    const ff r4 = ff_mul(r2, r2);
+    const ff r6 = ff_mul(r4, r2);
+    ff radial = ff_add(ff_make(1.0f), ff_mul_f(r2, S.k1));
+    radial = ff_add(radial, ff_mul_f(r4, S.k2));
+    radial = ff_add(radial, ff_mul_f(r6, S.k3));
+    const ff xy = ff_mul(x, y);
+    const ff pxy = ff_add(ff_mul_f(xy, S.p1), ff_mul_f(ff_add(r2, ff_mul_f(x2, 2.0f)), S.p2));
+    const ff pxy2 = ff_add(ff_mul_f(ff_add(r2, ff_mul_f(y2, 2.0f)), S.p1), ff_mul_f(xy, S.p2));
+    x = ff_add(ff_mul(x, radial), pxy);
+    y = ff_add(ff_mul(y, radial), pxy2);
+  }
+  *u0 = ff_add(ff_mul(S.ffx, x), S.fcx);
+  *v0 = ff_add(ff_mul(S.ffy, y), S.fcy);
+  return true;
+}
+
+// Bilinear read of the 2x2 footprint whose top-left texel is (x0, y0),
+// given as float texel indices; gather order is (x0,y1) (x1,y1) (x1,y0) (x0,y0).
+__device__ __forceinline__ float bilinear(cudaTextureObject_t tex, float x0, float y0, float fx, float fy) {
+  const float4 g = tex2Dgather<float4>(tex, x0 + 1.0f, y0 + 1.0f, 0);
+  const float top = fmaf(fx, g.z - g.w, g.w);
+  const float bot = fmaf(fx, g.y - g.x, g.x);
+  return fmaf(fy, bot - top, top);
+}
+
+__device__ __forceinline__ ViewResult ncc_from_moments(float n, float sr, float srr, float ss, float sss, float srs,
+                                                       int min_valid) {
+  ViewResult r{0.0f, 0};
+  if (n < (float)min_valid) return r;
+  const float inv_n = 1.0f / n;
+  const float mr = sr * inv_n, ms = ss * inv_n;
+  const float var_r = srr * inv_n - mr * mr;
+  const float var_s = sss * inv_n - ms * ms;
+  const float denom = sqrtf(var_r * var_s);
+  if (!(denom >= 1e-9f)) return r;
+  float ncc = (srs * inv_n - mr * ms) / denom;
+  ncc = fminf(1.0f, fmaxf(-1.0f, ncc));
+  r.ncc = ncc;
+  r.valid = 1;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// COMPAT: translated window (reference semantics)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ ViewResult eval_view_compat(const Job& J, const SrcView& S, int x, int y, const ff P[3],
+                                                       ff rho, float rho_f, const RefWindow& rw) {
+  ViewResult bad{0.0f, 0};
+  ff u0, v0;
+  float xz, mx, my;
+  if (!source_centre(S, P, rho, rho_f, &u0, &v0, &xz, &mx, &my)) return bad;
+  int iu, iv;
+  float fu, fv;
+  ff_floor_frac(u0, &iu, &fu);
+  ff_floor_frac(v0, &iv, &fv);
+  const int h = J.patch_half;
+  // valid rectangle: reference index x+0.5+dx in [0, W-1]; source index
+  // u0+dx in [0, Ws-1] (dx, dy integers)
+  const int dx_lo = max(-h, max(-x, -iu));
+  const int dx_hi = min(h, min(J.w - 2 - x, (fu == 0.0f ? S.w - 1 : S.w - 2) - iu));
+  const int dy_lo = max(-h, max(-y, -iv));
+  const int dy_hi = min(h, min(J.h - 2 - y, (fv == 0.0f ? S.h - 1 : S.h - 2) - iv));
+  const int nxv = dx_hi - dx_lo + 1, nyv = dy_hi - dy_lo + 1;
+  const int K = 2 * h + 1;
+  const int min_valid = J.min_valid;
+  if (nxv <= 0 || nyv <= 0 || nxv * nyv < min_valid) return bad;
+  // centre the source by its value at the window centre (or the nearest
+  // valid sample)
+  const int cdx = min(max(0, dx_lo), dx_hi), cdy = min(max(0, dy_lo), dy_hi);
+  const float sc = bilinear(S.tex, (float)(iu + cdx), (float)(iv + cdy), fu, fv);
+  const float rmean = rw.mean;
+  float sr = 0.f, srr = 0.f, ss = 0.f, sss = 0.f, srs = 0.f;
+  const bool full = rw.full && nxv == K && nyv == K;
+  for (int dy = dy_lo; dy <= dy_hi; ++dy) {
+    const float* rrow = J.ref_box + (size_t)(y + dy) * J.w + x;
+    const float gy = (float)(iv + dy);
+    float r_s = 0.f, r_ss = 0.f, r_rs = 0.f, r_r = 0.f, r_rr = 0.f;
+    for (int dx = dx_lo; dx <= dx_hi; ++dx) {
+      const float rv = __ldg(rrow + dx) - rmean;
+      const float sv = bilinear(S.tex, (float)(iu + dx), gy, fu, fv) - sc;
+      r_s += sv;
+      r_ss = fmaf(sv, sv, r_ss);
+      r_rs = fmaf(rv, sv, r_rs);
+      if (!full) {
+        r_r += rv;
+        r_rr = fmaf(rv, rv, r_rr);
+      }
+    }
+    ss += r_s;
+    sss += r_ss;
+    srs += r_rs;
+    sr += r_r;
+    srr += r_rr;
+  }
+  if (full) {
+    sr = 0.0f;
+    srr = rw.sxx;
+  }
+  return ncc_from_moments((float)(nxv * nyv), sr, srr, ss, sss, srs, min_valid);
+}
+
+// ---------------------------------------------------------------------------
+// PLANE: homography window
+// ---------------------------------------------------------------------------
+struct PlaneHyp {
+  float rho;          // inverse depth at the pixel centre
+  float nx, ny, nz;   // unit normal, reference camera frame
+  float kappa;        // n . ray(pixel centre)  (< 0 for a plane facing the camera)
+  float s0, s1;       // rho * nx / (fx kappa), rho * ny / (fy kappa)
+  float ex, ey;       // nx / fx, ny / fy   (n . ray changes by ex per dx)
+};
+
+__device__ __forceinline__ bool make_plane_hyp(const Job& J, float rx, float ry, float rho, float nx, float ny,
+                                               float nz, PlaneHyp* hp) {
+  const float kappa = nx * rx + ny * ry + nz;  // ray z = 1
+  // grazing or back-facing planes are not hypotheses
+  const float rn = sqrtf(rx * rx + ry * ry + 1.0f);
+  if (!(kappa < -0.05f * rn)) return false;
+  hp->rho = rho;
+  hp->nx = nx;
+  hp->ny = ny;
+  hp->nz = nz;
+  hp->kappa = kappa;
+  hp->ex = nx / J.rfx;
+  hp->ey = ny / J.rfy;
+  hp->s0 = rho * hp->ex / kappa;
+  hp->s1 = rho * hp->ey / kappa;
+  return true;
+}
+
+template <bool kFull>
+__device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int x, int y, int iu, int iv, float fu,
+                                             float fv, float A0, float A1, float B0, float B1, float c0, float c1,
+                                             const PlaneHyp& hp, float rmean, float sc, float* acc, float* cnt) {
+  const int h = J.patch_half;
+  float sr = 0.f, srr = 0.f, ss = 0.f, sss = 0.f, srs = 0.f, n = 0.f;
+  const float bu = (float)iu, bv = (float)iv;
+  const float umax = (float)(S.w - 1 - iu), vmax = (float)(S.h - 1 - iv);
+  const float umin = (float)(-iu), vmin = (float)(-iv);
+  for (int dy = -h; dy <= h; ++dy) {
+    const int ry = y + dy;
+    if (!kFull && (ry < 0 || ry >= J.h)) continue;
+    const float fdy = (float)dy;
+    float den = fmaf(fdy, c1, 1.0f - (float)h * c0);
+    float nu = fmaf(fdy, A1, -(float)h * A0);
+    float nv = fmaf(fdy, B1, -(float)h * B0);
+    float nr = hp.kappa + fdy * hp.ey - (float)h * hp.ex;
+    const float* rrow = J.ref + (size_t)ry * J.w + x;
+    float r_s = 0.f, r_ss = 0.f, r_rs = 0.f, r_r = 0.f, r_rr = 0.f, r_n = 0.f;
+#pragma unroll 4
+    for (int dx = -h; dx <= h; ++dx) {
+      const float rinv = __frcp_rn(den);
+      const float tu = fmaf(nu, rinv, fu);
+      const float tv = fmaf(nv, rinv, fv);
+      bool ok = true;
+      if (!kFull) {
+        const int rx = x + dx;
+        ok = rx >= 0 && rx < J.w && den > 0.0f && nr < 0.0f && tu >= umin && tu <= umax && tv >= vmin &&
+             tv <= vmax;
+      }
+      if (ok) {
+        const float flu = floorf(tu), flv = floorf(tv);
+        const float sv = bilinear(S.tex, bu + flu, bv + flv, tu - flu, tv - flv) - sc;
+        const float rv = __ldg(rrow + dx) - rmean;
+        r_s += sv;
+        r_ss = fmaf(sv, sv, r_ss);
+        r_rs = fmaf(rv, sv, r_rs);
+        if (!kFull) {
+          r_r += rv;
+          r_rr = fmaf(rv, rv, r_rr);
+          r_n += 1.0f;
+        }
+      }
+      den += c0;
+      nu += A0;
+      nv += B0;
+      nr += hp.ex;
+    }
+    ss += r_s;
+    sss += r_ss;
+    srs += r_rs;
+    sr += r_r;
+    srr += r_rr;
+    n += r_n;
+  }
+  acc[0] = sr;
+  acc[1] = srr;
+  acc[2] = ss;
+  acc[3] = sss;
+  acc[4] = srs;
+  *cnt = n;
+}
+
+__device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
+                                                      const PlaneHyp& hp, const RefWindow& rw) {
+  ViewResult bad{0.0f, 0};
+  ff u0, v0;
+  float xz, mx, my;
+  if (!source_centre(S, P, ff_make(hp.rho), hp.rho, &u0, &v0, &xz, &mx, &my)) return bad;
+  // per-sample offsets from the centre: du = (dx A0 + dy A1) / (1 + dx c0 + dy c1)
+  const float G0x = fmaf(hp.s0, S.b[0], S.Ac0[0]);
+  const float G0y = fmaf(hp.s0, S.b[1], S.Ac0[1]);
+  const float G0z = fmaf(hp.s0, S.b[2], S.Ac0[2]);
+  const float G1x = fmaf(hp.s1, S.b[0], S.Ac1[0]);
+  const float G1y = fmaf(hp.s1, S.b[1], S.Ac1[1]);
+  const float G1z = fmaf(hp.s1, S.b[2], S.Ac1[2]);
+  const float iz = 1.0f / xz;
+  const float A0 = S.fx * (G0x - mx * G0z) * iz;
+  const float A1 = S.fx * (G1x - mx * G1z) * iz;
+  const float B0 = S.fy * (G0y - my * G0z) * iz;
+  const float B1 = S.fy * (G1y - my * G1z) * iz;
+  const float c0 = G0z * iz;
+  const float c1 = G1z * iz;
+  // pixel-centre convention: index coordinate = coordinate - 0.5
+  int iu, iv;
+  float fu, fv;
+  ff_floor_frac(ff_add(u0, ff_make(-0.5f)), &iu, &fu);
+  ff_floor_frac(ff_add(v0, ff_make(-0.5f)), &iv, &fv);
+  const int h = J.patch_half;
+  const float fh = (float)h;
+  // fast path: the four corners (hence, by convexity, the whole window)
+  // inside the source, in front of it, and on the camera side of the plane
+  bool full = rw.full;
+  if (full) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float dx = (c & 1) ? fh : -fh, dy = (c & 2) ? fh : -fh;
+      const float den = fmaf(dx, c0, fmaf(dy, c1, 1.0f));
+      const float tu = fu + fmaf(dx, A0, dy * A1) / den;
+      const float tv = fv + fmaf(dx, B0, dy * B1) / den;
+      const float nr = hp.kappa + dx * hp.ex + dy * hp.ey;
+      full = full && den > 0.0f && nr < 0.0f && tu >= (float)(-iu) && tu <= (float)(S.w - 1 - iu) &&
+             tv >= (float)(-iv) && tv <= (float)(S.h - 1 - iv);
+    }
+  }
+  // source centring value: the sample at the window centre (clamped read)
+  const float sc = bilinear(S.tex, (float)iu, (float)iv, fu, fv);
+  float acc[5], n;
+  const int K = 2 * h + 1;
+  const int min_valid = J.min_valid;
+  if (full) {
+    plane_window<true>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+    return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
+  }
+  plane_window<false>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
+}
+
+// Reference-window statistics for a pixel: mean and centred sum of squares of
+// (I - 128) over the full K x K window (compat: of the box-filtered image).
+__device__ __forceinline__ RefWindow ref_window(const Job& J, int x, int y, bool compat) {
+  RefWindow rw;
+  const int h = J.patch_half;
+  const int wlim = compat ? J.w - 2 : J.w - 1;
+  const int hlim = compat ? J.h - 2 : J.h - 1;
+  const float* img = compat ? J.ref_box : J.ref;
+  int x0 = max(0, x - h), x1 = min(wlim, x + h), y0 = max(0, y - h), y1 = min(hlim, y + h);
+  rw.full = (x0 == x - h && x1 == x + h && y0 == y - h && y1 == y + h);
+  float s = 0.f;
+  int n = 0;
+  for (int yy = y0; yy <= y1; ++yy)
+    for (int xx = x0; xx <= x1; ++xx) {
+      s += __ldg(img + (size_t)yy * J.w + xx);
+      ++n;
+    }
+  rw.mean = n > 0 ? s / (float)n : 0.0f;
+  float q = 0.f;
+  for (int yy = y0; yy <= y1; ++yy) {
+    float qr = 0.f;
+    for (int xx = x0; xx <= x1; ++xx) {
+      const float d = __ldg(img + (size_t)yy * J.w + xx) - rw.mean;
+      qr = fmaf(d, d, qr);
+    }
+    q += qr;
+  }
+  rw.sxx = q;
+  return rw;
+}
+
+// P = A * ray for every source of the job, FP64 -> float-float.
+__device__ __forceinline__ void source_rays(const Job& J, const SrcView& S, const double ray[3], ff P[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double v = S.A[i * 3 + 0] * ray[0] + S.A[i * 3 + 1] * ray[1] + S.A[i * 3 + 2] * ray[2];
+    P[i] = ff_from_double(v);
+  }
+}
+
+}  // namespace rmvs

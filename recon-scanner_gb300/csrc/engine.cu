@@ -1,0 +1,1375 @@
+// engine.cu -- host runtime of the GB300 MVS engine and its C ABI
+// (include/recon_mvs_gb300.h).
+//
+// A Context owns one CUDA stream, reusable device workspaces and staged
+// jobs (one reference view each: source textures, reference images, camera
+// tables, search state).  Every entry point converts exceptions and CUDA
+// errors into recon_status codes at the boundary (the reference's Guard,
+// core/src/util/c_api.cpp:31-41); nothing here falls back to a CPU path.
+//
+// Host arithmetic that the bit-exact kernels depend on (relative transforms
+// for the consistency test, baselines) is compiled with -ffp-contract=off.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "kernels.h"
+#include "recon_mvs_gb300.h"
+
+namespace rmvs {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+thread_local std::string g_last_error;
+
+struct Failure : std::runtime_error {
+  recon_status code;
+  Failure(recon_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] static void fail(recon_status code, const std::string& msg) { throw Failure(code, msg); }
+
+static void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  if (e == cudaSuccess) return;
+  const std::string msg = std::string(what) + ": " + cudaGetErrorString(e) + " (" + file + ":" + std::to_string(line) + ")";
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    fail(RECON_ERR_OUT_OF_MEMORY, msg);
+  }
+  fail(RECON_ERR_MVS_GPU_FAILURE, msg);
+}
+#define CK(x) check_cuda((x), #x, __FILE__, __LINE__)
+
+template <class F>
+static recon_status guard(F&& fn) {
+  try {
+    fn();
+    g_last_error.clear();
+    return RECON_OK;
+  } catch (const Failure& f) {
+    g_last_error = f.what();
+    return f.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return RECON_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return RECON_ERR_INTERNAL;
+  } catch (...) {
+    g_last_error = "unknown exception";
+    return RECON_ERR_INTERNAL;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device memory
+// ---------------------------------------------------------------------------
+template <class T>
+struct DevArray {
+  T* p = nullptr;
+  size_t n = 0;
+  DevArray() = default;
+  DevArray(const DevArray&) = delete;
+  DevArray& operator=(const DevArray&) = delete;
+  ~DevArray() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    release();
+    CK(cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T)));
+    n = count;
+  }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void alloc(size_t b) {
+    if (b <= bytes && p) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    CK(cudaMallocHost(&p, std::max<size_t>(b, 1)));
+    bytes = b;
+  }
+};
+
+struct Texture {
+  cudaArray_t arr = nullptr;
+  cudaTextureObject_t tex = 0;
+  ~Texture() {
+    if (tex) cudaDestroyTextureObject(tex);
+    if (arr) cudaFreeArray(arr);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FP64 camera helpers in the reference's evaluation order
+// ---------------------------------------------------------------------------
+static void center_world(const recon_pose& p, double out[3]) {
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) s += p.r[j * 3 + i] * p.t[j];
+    out[i] = -s;
+  }
+}
+
+static double mean_baseline(const recon_pose& ref, const recon_pose* poses, const int32_t* idx, int n) {
+  double rc[3];
+  center_world(ref, rc);
+  double sum = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double sc[3], d[3];
+    center_world(poses[idx[k]], sc);
+    for (int i = 0; i < 3; ++i) d[i] = sc[i] - rc[i];
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) s += d[i] * d[i];
+    sum += std::sqrt(s);
+  }
+  return sum / (double)n;
+}
+
+// X_src = A X_ref + b with A = R_src R_ref^T, b = t_src - A t_ref
+static void relative_transform(const recon_pose& ref, const recon_pose& src, double A[9], double b[3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) s += src.r[i * 3 + q] * ref.r[j * 3 + q];
+      A[i * 3 + j] = s;
+    }
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) s += A[i * 3 + j] * ref.t[j];
+    b[i] = src.t[i] - s;
+  }
+}
+
+static ff ff_host(double d) {
+  const float hi = (float)d;
+  return ff{hi, (float)(d - (double)hi)};
+}
+
+static bool distorted(const recon_camera_intrinsics& k) {
+  return k.k1 != 0.0 || k.k2 != 0.0 || k.k3 != 0.0 || k.p1 != 0.0 || k.p2 != 0.0;
+}
+
+static double depth_to_inverse_depth(double d) { return d < 1e-9 ? 1e9 : 1.0 / d; }
+
+static int hardware_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return hw > 0 ? (int)hw : 1;
+}
+
+// ---------------------------------------------------------------------------
+// jobs
+// ---------------------------------------------------------------------------
+struct JobData {
+  int w = 0, h = 0, num_src = 0;
+  recon_mvs_config cfg{};
+  recon_mvs_options opts{};
+  bool degenerate = false;  // zero baseline or empty depth range: output all-invalid
+  double inv_per_px = 0.0;
+  DevArray<uint8_t> ref_u8;
+  DevArray<float> ref, ref_box;
+  std::vector<std::unique_ptr<Texture>> tex;
+  std::vector<SrcView> host_src;
+  DevArray<SrcView> src_table;
+  DevArray<float4> hyp;
+  DevArray<float> cost;
+  DevArray<uint8_t> support;
+  DevArray<double> inv[2];
+  DevArray<float> ccost[2];
+  DevArray<int32_t> csup[2];
+  std::vector<double> seeds;  // u, v, depth triples
+  DevArray<float> seed_depth;
+  int seed_gx = 0, seed_gy = 0;
+  DevArray<float> out_depth, out_conf, out_normal, out_cost;
+  DevArray<uint8_t> out_support;
+  DevArray<unsigned int> filled;
+  bool ran = false;
+  Job J{};
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  recon_mvs_options opts{};
+  std::map<int, std::unique_ptr<JobData>> jobs;
+  int next_id = 1;
+  DevArray<unsigned long long> counter;
+  DevArray<uint8_t> stage_u8;
+  DevArray<float> stage_f32;
+  DevArray<uint8_t> stage_tex;
+  size_t stage_tex_pitch = 0;
+  // compat draws (double-buffered)
+  PinnedBuf draws_host[2], fire_host[2];
+  DevArray<uint32_t> draws_dev[2];
+  DevArray<uint8_t> fire_dev[2];
+  cudaEvent_t copy_done[2] = {nullptr, nullptr};
+  cudaEvent_t ev_start = nullptr, ev_sweep0 = nullptr, ev_sweep1 = nullptr, ev_end = nullptr;
+  recon_mvs_stats stats{};
+
+  explicit Context(const recon_mvs_options& o) : opts(o) {
+    device = o.device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto& e : copy_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaEventCreate(&ev_start));
+    CK(cudaEventCreate(&ev_sweep0));
+    CK(cudaEventCreate(&ev_sweep1));
+    CK(cudaEventCreate(&ev_end));
+    counter.alloc(1);
+    CK(cudaMemsetAsync(counter.p, 0, sizeof(unsigned long long), stream));
+  }
+  ~Context() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    jobs.clear();
+    for (auto& e : copy_done)
+      if (e) cudaEventDestroy(e);
+    for (auto e : {ev_start, ev_sweep0, ev_sweep1, ev_end})
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  void use() const { CK(cudaSetDevice(device)); }
+};
+
+static void fill_defaults(recon_mvs_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->mode = RECON_MVS_MODE_PLANE;
+  o->storage = RECON_MVS_STORAGE_FP32;
+  o->best_k = 4;
+  o->refine = 1;
+  o->seed = 0x5DEECE66Dull;
+  o->device = 0;
+}
+
+// Contract checks of PatchMatchStereo (patchmatch_stereo.cpp:434-468).
+static bool intrinsics_global(const recon_mvs_views& v) { return v.num_src_intrinsics == v.num_src_poses; }
+
+static void validate_views(const recon_mvs_views* v) {
+  if (!v) fail(RECON_ERR_INVALID_ARGUMENT, "views is NULL");
+  if (!v->ref_gray || !v->ref_pose || !v->ref_intr) fail(RECON_ERR_INVALID_ARGUMENT, "reference image/pose/intrinsics NULL");
+  if (v->ref_w <= 0 || v->ref_h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "empty reference image");
+  if (v->num_src <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "no source views");
+  if (v->num_src > kMaxSources) fail(RECON_ERR_INVALID_ARGUMENT, "more than 32 source views");
+  if (!v->src_gray || !v->src_w || !v->src_h || !v->src_poses || !v->src_intrinsics || !v->source_indices)
+    fail(RECON_ERR_INVALID_ARGUMENT, "source arrays NULL");
+  const bool glob = intrinsics_global(*v);
+  const bool rel = v->num_src_intrinsics == v->num_src;
+  if (!glob && !rel) fail(RECON_ERR_INVALID_ARGUMENT, "src_intrinsics length is neither the pose count nor the source count");
+  for (int k = 0; k < v->num_src; ++k) {
+    const int si = v->source_indices[k];
+    if (si < 0 || si >= v->num_src_poses) fail(RECON_ERR_INVALID_ARGUMENT, "source index outside src_poses");
+    if (!v->src_gray[k] || v->src_w[k] <= 0 || v->src_h[k] <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "empty source image");
+  }
+}
+
+static const recon_camera_intrinsics& src_intr(const recon_mvs_views& v, int k) {
+  return intrinsics_global(v) ? v.src_intrinsics[v.source_indices[k]] : v.src_intrinsics[k];
+}
+
+static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32, int w, int h, bool fp16,
+                         Texture& T) {
+  cudaChannelFormatDesc desc = fp16 ? cudaCreateChannelDescHalf() : cudaCreateChannelDesc<float>();
+  CK(cudaMallocArray(&T.arr, &desc, w, h, cudaArrayTextureGather));
+  const size_t elem = fp16 ? 2 : 4;
+  const size_t pitch = ((size_t)w * elem + 255) & ~(size_t)255;
+  C.stage_tex.alloc(pitch * h);
+  if (is_f32)
+    CK(launch_prep_src_f32in((const float*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, fp16, C.stream));
+  else
+    CK(launch_prep_src((const uint8_t*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, fp16, C.stream));
+  CK(cudaMemcpy2DToArrayAsync(T.arr, 0, 0, C.stage_tex.p, pitch, (size_t)w * elem, h, cudaMemcpyDeviceToDevice,
+                              C.stream));
+  cudaResourceDesc rd;
+  std::memset(&rd, 0, sizeof(rd));
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = T.arr;
+  cudaTextureDesc td;
+  std::memset(&td, 0, sizeof(td));
+  td.addressMode[0] = cudaAddressModeClamp;
+  td.addressMode[1] = cudaAddressModeClamp;
+  td.filterMode = cudaFilterModePoint;
+  td.readMode = cudaReadModeElementType;
+  td.normalizedCoords = 0;
+  CK(cudaCreateTextureObject(&T.tex, &rd, &td, nullptr));
+}
+
+// Upload an 8-bit host image (optionally undistorted) to a device buffer;
+// returns a device pointer to either u8 or f32 data (is_f32 set).
+static const void* upload_image(Context& C, const uint8_t* host, int w, int h, const recon_camera_intrinsics* und,
+                                DevArray<uint8_t>& u8, DevArray<float>& f32, bool* is_f32) {
+  u8.alloc((size_t)w * h);
+  CK(cudaMemcpyAsync(u8.p, host, (size_t)w * h, cudaMemcpyHostToDevice, C.stream));
+  if (und && distorted(*und)) {
+    f32.alloc((size_t)w * h);
+    UndistortCam K{und->fx, und->fy, und->cx, und->cy, und->k1, und->k2, und->k3, und->p1, und->p2};
+    CK(launch_undistort(u8.p, w, h, K, f32.p, C.stream));
+    *is_f32 = true;
+    return f32.p;
+  }
+  *is_f32 = false;
+  return u8.p;
+}
+
+static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,
+                     const double* seeds, int num_seeds) {
+  validate_views(v);
+  if (!cfg) fail(RECON_ERR_INVALID_ARGUMENT, "config is NULL");
+  if (cfg->patch_size < 1) fail(RECON_ERR_INVALID_ARGUMENT, "patch_size < 1");
+  C.use();
+  auto jd = std::make_unique<JobData>();
+  JobData& D = *jd;
+  D.w = v->ref_w;
+  D.h = v->ref_h;
+  D.num_src = v->num_src;
+  D.cfg = *cfg;
+  D.opts = C.opts;
+  const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
+  const bool fp16 = C.opts.storage == RECON_MVS_STORAGE_FP16;
+  recon_camera_intrinsics rk = *v->ref_intr;
+  if (plane && !undistort) {
+    bool any = distorted(rk);
+    for (int k = 0; k < v->num_src; ++k) any = any || distorted(src_intr(*v, k));
+    if (any) fail(RECON_ERR_INVALID_ARGUMENT, "plane mode needs pinhole images: stage with undistort = 1");
+  }
+
+  // ---- reference image ----
+  bool ref_f32 = false;
+  DevArray<float> ref_und;
+  const void* ref_dev = upload_image(C, v->ref_gray, D.w, D.h, undistort ? &rk : nullptr, D.ref_u8, ref_und, &ref_f32);
+  D.ref.alloc((size_t)D.w * D.h);
+  const bool compat = !plane;
+  if (compat) D.ref_box.alloc((size_t)D.w * D.h);
+  if (ref_f32)
+    CK(launch_prep_ref_f32((const float*)ref_dev, D.w, D.h, D.ref.p, compat ? D.ref_box.p : nullptr, C.stream));
+  else
+    CK(launch_prep_ref((const uint8_t*)ref_dev, D.w, D.h, D.ref.p, compat ? D.ref_box.p : nullptr, C.stream));
+  if (undistort) rk.k1 = rk.k2 = rk.k3 = rk.p1 = rk.p2 = 0.0;
+
+  // ---- sources ----
+  D.host_src.resize(v->num_src);
+  for (int k = 0; k < v->num_src; ++k) {
+    recon_camera_intrinsics sk = src_intr(*v, k);
+    const recon_pose& sp = v->src_poses[v->source_indices[k]];
+    bool f32 = false;
+    DevArray<uint8_t> u8;
+    DevArray<float> fl;
+    const void* dev = upload_image(C, v->src_gray[k], v->src_w[k], v->src_h[k], undistort ? &sk : nullptr, u8, fl, &f32);
+    auto T = std::make_unique<Texture>();
+    make_texture(C, dev, f32, v->src_w[k], v->src_h[k], fp16, *T);
+    CK(cudaStreamSynchronize(C.stream));  // staging buffers are reused
+    if (undistort) sk.k1 = sk.k2 = sk.k3 = sk.p1 = sk.p2 = 0.0;
+    SrcView& S = D.host_src[k];
+    std::memset(&S, 0, sizeof(S));
+    S.tex = T->tex;
+    S.w = v->src_w[k];
+    S.h = v->src_h[k];
+    S.fx = (float)sk.fx;
+    S.fy = (float)sk.fy;
+    S.cx = (float)sk.cx;
+    S.cy = (float)sk.cy;
+    S.ffx = ff_host(sk.fx);
+    S.ffy = ff_host(sk.fy);
+    S.fcx = ff_host(sk.cx);
+    S.fcy = ff_host(sk.cy);
+    S.k1 = (float)sk.k1;
+    S.k2 = (float)sk.k2;
+    S.k3 = (float)sk.k3;
+    S.p1 = (float)sk.p1;
+    S.p2 = (float)sk.p2;
+    S.distorted = distorted(sk) ? 1 : 0;
+    double A[9], b[3];
+    relative_transform(*v->ref_pose, sp, A, b);
+    for (int i = 0; i < 9; ++i) S.A[i] = A[i];
+    for (int i = 0; i < 3; ++i) {
+      S.bd[i] = b[i];
+      S.b[i] = (float)b[i];
+      S.bff[i] = ff_host(b[i]);
+      S.Ac0[i] = (float)(A[i * 3 + 0] / rk.fx);
+      S.Ac1[i] = (float)(A[i * 3 + 1] / rk.fy);
+    }
+    D.tex.push_back(std::move(T));
+  }
+  D.src_table.alloc(v->num_src);
+  CK(cudaMemcpyAsync(D.src_table.p, D.host_src.data(), sizeof(SrcView) * v->num_src, cudaMemcpyHostToDevice, C.stream));
+
+  // ---- search range and baseline (patchmatch_stereo.cpp:473-485) ----
+  const double baseline = mean_baseline(*v->ref_pose, v->src_poses, v->source_indices, v->num_src);
+  const double inv_min = depth_to_inverse_depth(cfg->max_depth_m);
+  const double inv_max = depth_to_inverse_depth(cfg->min_depth_m);
+  D.degenerate = baseline < 1e-9 || !(inv_max > inv_min) || inv_min <= 0.0;
+  const double focal_px = 0.5 * (rk.fx + rk.fy);
+  D.inv_per_px = 1.0 / (focal_px * baseline);
+
+  Job& J = D.J;
+  std::memset(&J, 0, sizeof(J));
+  J.w = D.w;
+  J.h = D.h;
+  J.num_src = v->num_src;
+  J.patch_half = cfg->patch_size / 2;
+  J.min_valid = cfg->patch_size * cfg->patch_size / 2;
+  J.rfx = (float)rk.fx;
+  J.rfy = (float)rk.fy;
+  J.rcx = (float)rk.cx;
+  J.rcy = (float)rk.cy;
+  J.drfx = rk.fx;
+  J.drfy = rk.fy;
+  J.drcx = rk.cx;
+  J.drcy = rk.cy;
+  J.ref_distorted = distorted(rk) ? 1 : 0;
+  J.rk1 = rk.k1;
+  J.rk2 = rk.k2;
+  J.rk3 = rk.k3;
+  J.rp1 = rk.p1;
+  J.rp2 = rk.p2;
+  J.ref = D.ref.p;
+  J.ref_box = D.ref_box.p;
+  J.src = D.src_table.p;
+  J.dinv_min = inv_min;
+  J.dinv_max = inv_max;
+  J.rho_min = (float)inv_min;
+  J.rho_max = (float)inv_max;
+  J.min_depth = cfg->min_depth_m;
+  J.max_depth = cfg->max_depth_m;
+  J.photo_threshold = (float)cfg->photo_threshold;
+  J.best_k = C.opts.best_k;
+  J.seed = C.opts.seed;
+  J.eval_counter = C.counter.p;
+
+  const size_t npx = (size_t)D.w * D.h;
+  if (plane) {
+    D.hyp.alloc(npx);
+    D.cost.alloc(npx);
+    D.support.alloc(npx);
+    J.hyp = D.hyp.p;
+    J.cost = D.cost.p;
+    J.support = D.support.p;
+  } else {
+    for (int i = 0; i < 2; ++i) {
+      D.inv[i].alloc(npx);
+      D.ccost[i].alloc(npx);
+      D.csup[i].alloc(npx);
+    }
+    J.inv = D.inv[0].p;
+    J.isupport = D.csup[0].p;
+  }
+  if (seeds && num_seeds > 0) D.seeds.assign(seeds, seeds + 3 * (size_t)num_seeds);
+  D.out_depth.alloc(npx);
+  D.out_conf.alloc(npx);
+  D.out_support.alloc(npx);
+  if (plane) {
+    D.out_normal.alloc(npx * 3);
+  }
+  D.out_cost.alloc(npx);
+  D.filled.alloc(1);
+  CK(cudaStreamSynchronize(C.stream));
+  const int id = C.next_id++;
+  C.jobs[id] = std::move(jd);
+  return id;
+}
+
+static JobData& get_job(Context& C, int id) {
+  auto it = C.jobs.find(id);
+  if (it == C.jobs.end()) fail(RECON_ERR_INVALID_ARGUMENT, "unknown job id");
+  return *it->second;
+}
+
+// Seeds -> per-32-px-cell mean depth (patchmatch_stereo.cpp:499-533).
+static void cell_depths(const JobData& D, std::vector<double>* cell_sum, std::vector<int>* cell_n, int* gx, int* gy) {
+  const int grid = 32;
+  *gx = (D.w + grid - 1) / grid;
+  *gy = (D.h + grid - 1) / grid;
+  cell_sum->assign((size_t)(*gx) * (*gy), 0.0);
+  cell_n->assign((size_t)(*gx) * (*gy), 0);
+  for (size_t i = 0; i + 2 < D.seeds.size(); i += 3) {
+    const double su = D.seeds[i], sv = D.seeds[i + 1], sd = D.seeds[i + 2];
+    if (su < 0 || sv < 0 || su >= D.w || sv >= D.h) continue;
+    if (sd <= 0.0) continue;
+    const int cx = std::min(*gx - 1, (int)su / grid);
+    const int cy = std::min(*gy - 1, (int)sv / grid);
+    (*cell_sum)[(size_t)cy * (*gx) + cx] += sd;
+    (*cell_n)[(size_t)cy * (*gx) + cx] += 1;
+  }
+}
+
+// ---- plane mode -----------------------------------------------------------
+static void run_plane(Context& C, JobData& D) {
+  Job& J = D.J;
+  const float* seed_ptr = nullptr;
+  if (!D.seeds.empty()) {
+    std::vector<double> sum;
+    std::vector<int> cnt;
+    int gx, gy;
+    cell_depths(D, &sum, &cnt, &gx, &gy);
+    std::vector<float> sd(sum.size(), 0.f);
+    for (size_t i = 0; i < sum.size(); ++i)
+      if (cnt[i] > 0) sd[i] = (float)(sum[i] / (double)cnt[i]);
+    D.seed_depth.alloc(sd.size());
+    CK(cudaMemcpyAsync(D.seed_depth.p, sd.data(), sd.size() * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+    D.seed_gx = gx;
+    seed_ptr = D.seed_depth.p;
+  }
+  CK(cudaEventRecord(C.ev_start, C.stream));
+  CK(launch_plane_init(J, seed_ptr, 32, D.seed_gx, C.stream));
+  CK(cudaEventRecord(C.ev_sweep0, C.stream));
+  int launches = 0;
+  for (int it = 0; it < D.cfg.iterations; ++it) {
+    CK(launch_plane_sweep(J, 0, it, D.cfg.iterations, C.stream));
+    CK(launch_plane_sweep(J, 1, it, D.cfg.iterations, C.stream));
+    launches += 2;
+  }
+  CK(cudaEventRecord(C.ev_sweep1, C.stream));
+  if (D.opts.refine && D.cfg.subpixel_iterations > 0)
+    CK(launch_plane_refine(J, D.inv_per_px, D.cfg.subpixel_iterations, C.stream));
+  CK(cudaMemsetAsync(D.filled.p, 0, sizeof(unsigned int), C.stream));
+  CK(launch_plane_output(J, D.out_depth.p, D.out_support.p, D.out_conf.p, D.out_normal.p, D.out_cost.p, D.filled.p,
+                         C.stream));
+  CK(cudaEventRecord(C.ev_end, C.stream));
+  C.stats.last_sweep_launches = launches;
+}
+
+// ---- compat mode ----------------------------------------------------------
+// The reference's random init (one global xorshift in row-major order after
+// seeding, :487-539) and its per-sweep row-block draws (:612-660).
+struct XorShift {
+  uint64_t s;
+  explicit XorShift(uint64_t seed) : s(seed ? seed : 0x9E3779B97F4A7C15ull) {}
+  uint32_t next() {
+    s ^= s >> 12;
+    s ^= s << 25;
+    s ^= s >> 27;
+    return (uint32_t)((s * 0x2545F4914F6CDD1Dull) >> 32);
+  }
+};
+
+static int resolve_threads(const recon_mvs_config& c) {
+  int t = c.num_threads;
+  if (t <= 0) t = hardware_threads();
+  return std::max(1, t);
+}
+
+static void gen_draws(const JobData& D, int iter, int dir, uint32_t* draws, uint8_t* fire) {
+  const int W = D.w, H = D.h;
+  const int count = D.cfg.random_search_count > 0 ? D.cfg.random_search_count : 0;
+  const int stride = count + 1;
+  const int threads = resolve_threads(D.cfg);
+  const int block_count = std::min(threads, std::max(1, H / 16));
+  const int rows_per_block = (H + block_count - 1) / block_count;
+  const bool reverse_x = (dir == 1 || dir == 3);
+  const bool reverse_y = (dir >= 2);
+  const double restart = D.cfg.restart_ratio;
+  auto one = [&](int b) {
+    const int yb0 = b * rows_per_block;
+    const int yb1 = std::min(H, yb0 + rows_per_block);
+    if (yb0 >= yb1) return;
+    XorShift rng(0x5DEECE66Dull + (uint64_t)b * 0x9E3779B97F4A7C15ull + (uint64_t)iter * 0xC2B2AE3D27D4EB4Full);
+    const int y_start = reverse_y ? yb1 - 1 : yb0, y_end = reverse_y ? yb0 - 1 : yb1, y_step = reverse_y ? -1 : 1;
+    for (int y = y_start; y != y_end; y += y_step) {
+      const int x_start = reverse_x ? W - 1 : 0, x_end = reverse_x ? -1 : W, x_step = reverse_x ? -1 : 1;
+      for (int x = x_start; x != x_end; x += x_step) {
+        const size_t idx = (size_t)y * W + x;
+        uint32_t* d = draws + idx * stride;
+        for (int k = 0; k < count; ++k) d[k] = rng.next();
+        const uint32_t t = rng.next();
+        const bool f = ((double)t / 4294967296.0) < restart;
+        fire[idx] = f ? 1 : 0;
+        d[count] = f ? rng.next() : 0u;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int b = 1; b < block_count; ++b) pool.emplace_back(one, b);
+  one(0);
+  for (auto& t : pool) t.join();
+}
+
+static void run_compat(Context& C, JobData& D) {
+  Job& J = D.J;
+  const size_t npx = (size_t)D.w * D.h;
+  // initial inverse depths (host, the reference's generator)
+  std::vector<double> inv(npx, 0.0);
+  std::vector<uint8_t> init(npx, 0);
+  if (!D.seeds.empty()) {
+    std::vector<double> sum;
+    std::vector<int> cnt;
+    int gx, gy;
+    cell_depths(D, &sum, &cnt, &gx, &gy);
+    for (int y = 0; y < D.h; ++y)
+      for (int x = 0; x < D.w; ++x) {
+        const int cx = std::min(gx - 1, x / 32), cy = std::min(gy - 1, y / 32);
+        const size_t c = (size_t)cy * gx + cx;
+        if (cnt[c] == 0) continue;
+        inv[(size_t)y * D.w + x] = depth_to_inverse_depth(sum[c] / (double)cnt[c]);
+        init[(size_t)y * D.w + x] = 1;
+      }
+  }
+  XorShift rng(0x5DEECE66Dull);
+  for (size_t i = 0; i < npx; ++i) {
+    if (init[i]) continue;
+    inv[i] = J.dinv_min + ((double)rng.next() / 4294967296.0) * (J.dinv_max - J.dinv_min);
+  }
+  CK(cudaEventRecord(C.ev_start, C.stream));
+  CK(cudaMemcpyAsync(D.inv[0].p, inv.data(), npx * sizeof(double), cudaMemcpyHostToDevice, C.stream));
+  J.inv = D.inv[0].p;
+  J.isupport = D.csup[0].p;
+  CK(launch_compat_init(J, D.ccost[0].p, C.stream));
+  CK(cudaEventRecord(C.ev_sweep0, C.stream));
+  const int count = std::max(0, D.cfg.random_search_count);
+  const int stride = count + 1;
+  const int dirs = std::max(1, D.cfg.propagation_directions);
+  int cur = 0, sweep = 0;
+  for (int it = 0; it < D.cfg.iterations; ++it)
+    for (int dir = 0; dir < dirs; ++dir, ++sweep) {
+      const int j = sweep & 1;
+      if (sweep >= 2) CK(cudaEventSynchronize(C.copy_done[j]));
+      C.draws_host[j].alloc(npx * stride * sizeof(uint32_t));
+      C.fire_host[j].alloc(npx);
+      gen_draws(D, it, dir, (uint32_t*)C.draws_host[j].p, (uint8_t*)C.fire_host[j].p);
+      C.draws_dev[j].alloc(npx * stride);
+      C.fire_dev[j].alloc(npx);
+      CK(cudaMemcpyAsync(C.draws_dev[j].p, C.draws_host[j].p, npx * stride * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                         C.stream));
+      CK(cudaMemcpyAsync(C.fire_dev[j].p, C.fire_host[j].p, npx, cudaMemcpyHostToDevice, C.stream));
+      CK(cudaEventRecord(C.copy_done[j], C.stream));
+      const int nxt = cur ^ 1;
+      CK(launch_compat_sweep(J, D.inv[cur].p, D.ccost[cur].p, D.csup[cur].p, D.inv[nxt].p, D.ccost[nxt].p,
+                             D.csup[nxt].p, C.draws_dev[j].p, C.fire_dev[j].p, stride, count,
+                             D.cfg.random_search_radius_ratio, D.cfg.propagation_enabled, C.stream));
+      cur = nxt;
+    }
+  CK(cudaEventRecord(C.ev_sweep1, C.stream));
+  CK(cudaMemsetAsync(D.filled.p, 0, sizeof(unsigned int), C.stream));
+  CK(launch_compat_output(J, D.inv[cur].p, D.ccost[cur].p, D.csup[cur].p, D.out_depth.p, D.out_support.p,
+                          D.out_conf.p, D.filled.p, C.stream));
+  CK(cudaMemcpyAsync(D.out_cost.p, D.ccost[cur].p, npx * sizeof(float), cudaMemcpyDeviceToDevice, C.stream));
+  CK(cudaEventRecord(C.ev_end, C.stream));
+  C.stats.last_sweep_launches = sweep;
+}
+
+static void run_job(Context& C, JobData& D) {
+  C.use();
+  if (D.degenerate) {
+    D.ran = true;
+    return;
+  }
+  if (D.opts.mode == RECON_MVS_MODE_PLANE)
+    run_plane(C, D);
+  else
+    run_compat(C, D);
+  D.ran = true;
+}
+
+static void finish_stats(Context& C) {
+  float ms = 0.f, sw = 0.f;
+  if (cudaEventElapsedTime(&ms, C.ev_start, C.ev_end) == cudaSuccess) C.stats.last_run_ms = ms;
+  if (cudaEventElapsedTime(&sw, C.ev_sweep0, C.ev_sweep1) == cudaSuccess) C.stats.last_sweep_ms = sw;
+  cudaGetLastError();
+}
+
+static void download_job(Context& C, JobData& D, recon_mvs_depth_map* out, uint32_t* filled) {
+  if (!out || !out->depth || !out->support_count || !out->confidence)
+    fail(RECON_ERR_INVALID_ARGUMENT, "output depth map arrays NULL");
+  if (out->width != D.w || out->height != D.h) fail(RECON_ERR_INVALID_ARGUMENT, "output depth map size mismatch");
+  const size_t npx = (size_t)D.w * D.h;
+  if (!D.ran) fail(RECON_ERR_INVALID_ARGUMENT, "job has not run");
+  if (D.degenerate) {
+    CK(cudaStreamSynchronize(C.stream));
+    const float nan = std::nanf("");
+    std::fill(out->depth, out->depth + npx, nan);
+    std::memset(out->support_count, 0, npx);
+    std::fill(out->confidence, out->confidence + npx, 0.0f);
+    if (out->normal) std::fill(out->normal, out->normal + 3 * npx, 0.0f);
+    if (out->cost) std::fill(out->cost, out->cost + npx, 1e30f);
+    if (filled) *filled = 0;
+    return;
+  }
+  CK(cudaMemcpyAsync(out->depth, D.out_depth.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->support_count, D.out_support.p, npx, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->confidence, D.out_conf.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  if (out->normal) {
+    if (D.out_normal.p)
+      CK(cudaMemcpyAsync(out->normal, D.out_normal.p, 3 * npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    else
+      std::fill(out->normal, out->normal + 3 * npx, 0.0f);
+  }
+  if (out->cost) CK(cudaMemcpyAsync(out->cost, D.out_cost.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  unsigned int f = 0;
+  CK(cudaMemcpyAsync(&f, D.filled.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  finish_stats(C);
+  unsigned long long ev = 0;
+  CK(cudaMemcpy(&ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
+  C.stats.hypotheses_evaluated = ev;
+  if (filled) *filled = f;
+}
+
+// ---------------------------------------------------------------------------
+// default per-thread contexts for the stateless entry points
+// ---------------------------------------------------------------------------
+static Context& default_context(const recon_mvs_options* opts) {
+  thread_local std::map<std::string, std::unique_ptr<Context>> ctxs;
+  recon_mvs_options o;
+  if (opts)
+    o = *opts;
+  else
+    fill_defaults(&o);
+  const std::string key((const char*)&o, sizeof(o));
+  auto it = ctxs.find(key);
+  if (it == ctxs.end()) it = ctxs.emplace(key, std::make_unique<Context>(o)).first;
+  return *it->second;
+}
+
+struct JobScope {
+  Context& C;
+  int id;
+  ~JobScope() { C.jobs.erase(id); }
+};
+
+// ---------------------------------------------------------------------------
+// parameter registry (params.cpp:386-422) and the StageMvs mapping
+// (orchestrator.cpp:952-970)
+// ---------------------------------------------------------------------------
+enum class PType { kInt, kDouble };
+struct PSpec {
+  const char* key;
+  PType type;
+  double def, fast, std_, high, lo, hi;
+};
+static const PSpec kSpecs[] = {
+    {"mvs_patch_size", PType::kInt, 7, 7, 7, 11, 3, 21},
+    {"mvs_patch_iterations", PType::kInt, 3, 3, 3, 6, 1, 20},
+    {"mvs_patch_random_search_radius", PType::kInt, 2, 2, 2, 4, 0, 16},
+    {"mvs_num_views", PType::kInt, 5, 5, 5, 8, 2, 32},
+    {"mvs_subpixel_iterations", PType::kInt, 3, 2, 3, 5, 0, 10},
+    {"mvs_geo_consistency_threshold", PType::kDouble, 0.02, 0.02, 0.02, 0.01, 0.001, 0.20},
+    {"mvs_photo_threshold", PType::kDouble, 0.2, 0.2, 0.2, 0.1, 0.01, 1.0},
+    {"mvs_fusion_voxel_size_m", PType::kDouble, 0.001, 0.002, 0.001, 0.0005, 0.0002, 0.005},
+    {"mvs_image_scale", PType::kDouble, 1.0, 1.0, 1.0, 1.0, 0.25, 1.0},
+    {"mvs_min_depth_m", PType::kDouble, 0.10, 0.10, 0.10, 0.10, 0.02, 1.0},
+    {"mvs_max_depth_m", PType::kDouble, 1.50, 1.50, 1.50, 2.00, 0.2, 5.0},
+    {"mvs_gpu_tile_size", PType::kInt, 256, 256, 256, 128, 32, 1024},
+    {"mvs_pm_search_radius_ratio", PType::kDouble, 0.30, 0.40, 0.30, 0.22, 0.01, 1.0},
+    {"mvs_subpixel_window_ratio", PType::kDouble, 0.50, 0.70, 0.50, 0.35, 0.05, 4.0},
+    {"mvs_num_threads", PType::kInt, 0, 0, 0, 0, 0, 64},
+    // not an mvs_* key, but StageMvs takes num_threads from it (:970)
+    {"perf_thread_pool_size", PType::kInt, 0, 0, 0, 0, 0, 64},
+};
+
+static void apply_mapped(recon_mvs_config* c, const std::string& key, double v) {
+  if (key == "mvs_num_views") c->num_views = (int32_t)v;
+  else if (key == "mvs_photo_threshold") c->photo_threshold = v;
+  else if (key == "mvs_geo_consistency_threshold") c->geo_consistency_threshold = v;
+  // StageMvs feeds the integer radius key into the ratio field (:959-960)
+  else if (key == "mvs_patch_random_search_radius") c->random_search_radius_ratio = v;
+  else if (key == "mvs_patch_size") c->patch_size = (int32_t)v;
+  else if (key == "mvs_patch_iterations") c->iterations = (int32_t)v;
+  else if (key == "mvs_subpixel_iterations") c->subpixel_iterations = (int32_t)v;
+  else if (key == "mvs_min_depth_m") c->min_depth_m = v;
+  else if (key == "mvs_max_depth_m") c->max_depth_m = v;
+  else if (key == "mvs_fusion_voxel_size_m") c->fusion_voxel_size_m = v;
+  else if (key == "perf_thread_pool_size") c->num_threads = (int32_t)v;
+  // registered but not read by StageMvs: mvs_image_scale, mvs_gpu_tile_size,
+  // mvs_pm_search_radius_ratio, mvs_subpixel_window_ratio, mvs_num_threads
+}
+
+}  // namespace rmvs
+
+using namespace rmvs;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+RECON_API uint32_t recon_mvs_abi_version(void) { return RECON_MVS_GB300_ABI_VERSION; }
+
+RECON_API const char* recon_mvs_last_error(void) { return g_last_error.c_str(); }
+
+RECON_API void recon_mvs_config_default(recon_mvs_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->num_views = 7;
+  c->ref_view_index = -1;
+  c->ideal_angle_min_deg = 8.0;
+  c->ideal_angle_max_deg = 35.0;
+  c->max_view_scale_mismatch = 0.15;
+  c->view_angle_weight = 1.0;
+  c->view_texture_weight = 0.8;
+  c->view_spread_weight = 0.6;
+  c->view_scale_weight = 0.4;
+  c->reference_depth_m = 0.40;
+  c->patch_size = 11;
+  c->iterations = 4;
+  c->random_search_count = 5;
+  c->random_search_radius_ratio = 0.30;
+  c->restart_ratio = 0.05;
+  c->propagation_directions = 4;
+  c->propagation_enabled = 1;
+  c->num_threads = 0;
+  c->photo_threshold = 1.0;
+  c->depth_regularization = 0.02;
+  c->geo_consistency_threshold = 0.02;
+  c->weak_texture_variance = 12.0;
+  c->subpixel_iterations = 4;
+  c->subpixel_fit_points = 5;
+  c->subpixel_window_ratio = 0.005;
+  c->min_depth_m = 0.10;
+  c->max_depth_m = 1.50;
+  c->min_view_consistency = 2;
+  c->fusion_voxel_size_m = 0.001;
+}
+
+RECON_API void recon_mvs_options_default(recon_mvs_options* o) {
+  if (o) fill_defaults(o);
+}
+
+RECON_API recon_status recon_mvs_config_set_param(recon_mvs_config* cfg, const char* key, int32_t value_int,
+                                                  double value_double) {
+  return guard([&] {
+    if (!cfg || !key) fail(RECON_ERR_INVALID_ARGUMENT, "NULL config or key");
+    const PSpec* spec = nullptr;
+    for (const auto& s : kSpecs)
+      if (std::strcmp(s.key, key) == 0) spec = &s;
+    if (!spec) fail(RECON_ERR_INVALID_ARGUMENT, std::string("unknown parameter ") + key);
+    double v = spec->type == PType::kDouble ? value_double : (double)value_int;
+    if (std::isnan(v) || std::isinf(v)) v = spec->lo;
+    v = std::min(std::max(v, spec->lo), spec->hi);
+    if (spec->type == PType::kInt) v = std::nearbyint(v);
+    apply_mapped(cfg, key, v);
+  });
+}
+
+RECON_API recon_status recon_mvs_config_apply_preset(recon_mvs_config* cfg, int32_t preset) {
+  return guard([&] {
+    if (!cfg || preset < 0 || preset > 2) fail(RECON_ERR_INVALID_ARGUMENT, "bad preset");
+    for (const auto& s : kSpecs) {
+      const double v = preset == 0 ? s.fast : (preset == 1 ? s.std_ : s.high);
+      apply_mapped(cfg, s.key, v);
+    }
+  });
+}
+
+RECON_API recon_status recon_mvs_select_source_views(const recon_pose* ref_pose, const recon_pose* poses,
+                                                     int32_t num_poses, const recon_camera_intrinsics* intr,
+                                                     const recon_mvs_config* cfg, int32_t* out_indices,
+                                                     int32_t capacity, int32_t* out_count) {
+  return guard([&] {
+    (void)intr;
+    if (!ref_pose || (!poses && num_poses > 0) || !cfg || !out_count) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    struct Cand {
+      int index;
+      double score;
+    };
+    std::vector<Cand> cands;
+    double rc[3];
+    center_world(*ref_pose, rc);
+    const double kPi = 3.14159265358979323846;
+    for (int i = 0; i < num_poses; ++i) {
+      if (i == cfg->ref_view_index) continue;
+      double sc[3], base[3];
+      center_world(poses[i], sc);
+      for (int q = 0; q < 3; ++q) base[q] = sc[q] - rc[q];
+      double bl = 0.0;
+      for (int q = 0; q < 3; ++q) bl += base[q] * base[q];
+      if (std::sqrt(bl) < 1e-6) continue;
+      const double z_ref = cfg->reference_depth_m;
+      const double z_src = z_ref + base[2];
+      if (z_src <= 1e-6) continue;
+      if (std::fabs(z_ref / z_src - 1.0) > cfg->max_view_scale_mismatch) continue;
+      double rel[3];
+      for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int q = 0; q < 3; ++q) s += ref_pose->r[r * 3 + q] * base[q];
+        rel[r] = s;
+      }
+      double dd = 0.0;
+      for (int q = 0; q < 3; ++q) dd += rel[q] * rel[q];
+      const double dist = std::sqrt(dd);
+      if (dist < 1e-6) continue;
+      const double angle = std::acos(std::clamp(rel[2] / dist, -1.0, 1.0)) * 180.0 / kPi;
+      double score;
+      if (angle < cfg->ideal_angle_min_deg)
+        score = angle / cfg->ideal_angle_min_deg;
+      else if (angle > cfg->ideal_angle_max_deg)
+        score = std::max(0.0, 1.0 - (angle - cfg->ideal_angle_max_deg) / (cfg->ideal_angle_max_deg * 2.0));
+      else
+        score = 1.0;
+      cands.push_back({i, score * cfg->view_angle_weight});
+    }
+    // the same library sort as the reference (:194-197)
+    std::sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.score > b.score; });
+    int n = 0;
+    for (size_t i = 0; i < cands.size() && n < cfg->num_views; ++i) {
+      if (out_indices && n < capacity) out_indices[n] = cands[i].index;
+      ++n;
+    }
+    *out_count = std::min(n, std::max(0, capacity));
+  });
+}
+
+RECON_API recon_status recon_mvs_compute_ncc(const uint8_t* ref, int32_t ref_w, int32_t ref_h, const uint8_t* src,
+                                             int32_t src_w, int32_t src_h, const double* coords, int32_t n,
+                                             int32_t patch_size, recon_mvs_ncc_result* out) {
+  return guard([&] {
+    if (!ref || !src || (!coords && n > 0) || (!out && n > 0)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (ref_w <= 0 || ref_h <= 0 || src_w <= 0 || src_h <= 0 || n < 0) fail(RECON_ERR_INVALID_ARGUMENT, "bad size");
+    if (n == 0) return;
+    Context& C = default_context(nullptr);
+    C.use();
+    DevArray<uint8_t> dr, ds;
+    DevArray<NccWindow> dw;
+    DevArray<int> dv, dk, dn;
+    DevArray<double> dc;
+    dr.alloc((size_t)ref_w * ref_h);
+    ds.alloc((size_t)src_w * src_h);
+    dw.alloc(n);
+    dv.alloc(n);
+    dk.alloc(n);
+    dn.alloc(n);
+    dc.alloc(n);
+    CK(cudaMemcpyAsync(dr.p, ref, (size_t)ref_w * ref_h, cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(ds.p, src, (size_t)src_w * src_h, cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(dw.p, coords, sizeof(NccWindow) * n, cudaMemcpyHostToDevice, C.stream));
+    CK(launch_ncc_windows(dr.p, ref_w, ref_h, ds.p, src_w, src_h, patch_size, n, dw.p, dv.p, dc.p, dk.p, dn.p,
+                          C.stream));
+    std::vector<int> v(n), k(n), s(n);
+    std::vector<double> c(n);
+    CK(cudaMemcpyAsync(v.data(), dv.p, n * sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(k.data(), dk.p, n * sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(s.data(), dn.p, n * sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(c.data(), dc.p, n * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    for (int i = 0; i < n; ++i) out[i] = recon_mvs_ncc_result{v[i], c[i], k[i], s[i]};
+  });
+}
+
+RECON_API recon_status recon_mvs_evaluate(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                          const recon_mvs_options* opts, int32_t n, const int32_t* px,
+                                          const int32_t* py, const double* inv_depth, const float* normals,
+                                          float* out_cost, int32_t* out_support, float* out_view_cost) {
+  return guard([&] {
+    if (n < 0 || (n > 0 && (!px || !py || !inv_depth || !out_cost || !out_support)))
+      fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    Context& C = default_context(opts);
+    const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
+    if (plane && n > 0 && !normals) fail(RECON_ERR_INVALID_ARGUMENT, "plane mode needs normals");
+    const int id = stage_job(C, views, cfg, false, nullptr, 0);
+    JobScope scope{C, id};
+    if (n == 0) return;
+    JobData& D = get_job(C, id);
+    for (int i = 0; i < n; ++i)
+      if (px[i] < 0 || py[i] < 0 || px[i] >= D.w || py[i] >= D.h) fail(RECON_ERR_INVALID_ARGUMENT, "pixel outside image");
+    DevArray<int> dx, dy, ds;
+    DevArray<double> di;
+    DevArray<float> dn, dc, dv;
+    dx.alloc(n);
+    dy.alloc(n);
+    ds.alloc(n);
+    di.alloc(n);
+    dc.alloc(n);
+    CK(cudaMemcpyAsync(dx.p, px, n * sizeof(int), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(dy.p, py, n * sizeof(int), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(di.p, inv_depth, n * sizeof(double), cudaMemcpyHostToDevice, C.stream));
+    if (plane) {
+      dn.alloc((size_t)n * 3);
+      CK(cudaMemcpyAsync(dn.p, normals, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+    }
+    if (out_view_cost) dv.alloc((size_t)n * D.num_src);
+    CK(launch_eval_hyps(D.J, plane ? 1 : 0, n, dx.p, dy.p, di.p, dn.p, dc.p, ds.p, out_view_cost ? dv.p : nullptr,
+                        C.stream));
+    CK(cudaMemcpyAsync(out_cost, dc.p, n * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out_support, ds.p, n * sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    if (out_view_cost)
+      CK(cudaMemcpyAsync(out_view_cost, dv.p, (size_t)n * D.num_src * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+RECON_API recon_status recon_mvs_patchmatch(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                            const recon_mvs_options* opts, const double* seed_points,
+                                            int32_t num_seeds, recon_mvs_depth_map* out, uint32_t* out_filled) {
+  return guard([&] {
+    if (!out) fail(RECON_ERR_INVALID_ARGUMENT, "out is NULL");
+    Context& C = default_context(opts);
+    const int id = stage_job(C, views, cfg, false, seed_points, num_seeds);
+    JobScope scope{C, id};
+    JobData& D = get_job(C, id);
+    run_job(C, D);
+    download_job(C, D, out, out_filled);
+  });
+}
+
+RECON_API recon_status recon_mvs_refine_subpixel(const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                                 const recon_mvs_options* opts, recon_mvs_depth_map* depth,
+                                                 uint32_t* out_refined) {
+  return guard([&] {
+    if (!depth || !depth->depth || !depth->confidence) fail(RECON_ERR_INVALID_ARGUMENT, "depth map NULL");
+    recon_mvs_options o;
+    if (opts)
+      o = *opts;
+    else
+      fill_defaults(&o);
+    o.mode = RECON_MVS_MODE_COMPAT;  // RefineSubpixel's cost is the reference's
+    Context& C = default_context(&o);
+    const int id = stage_job(C, views, cfg, false, nullptr, 0);
+    JobScope scope{C, id};
+    JobData& D = get_job(C, id);
+    if (depth->width != D.w || depth->height != D.h) fail(RECON_ERR_INVALID_ARGUMENT, "depth map size mismatch");
+    if (out_refined) *out_refined = 0;
+    const double baseline = mean_baseline(*views->ref_pose, views->src_poses, views->source_indices, views->num_src);
+    if (baseline < 1e-9) return;  // the reference returns 0 (:786)
+    const size_t npx = (size_t)D.w * D.h;
+    CK(cudaMemcpyAsync(D.out_depth.p, depth->depth, npx * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(D.out_conf.p, depth->confidence, npx * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemsetAsync(D.filled.p, 0, sizeof(unsigned int), C.stream));
+    CK(launch_compat_refine(D.J, D.out_depth.p, D.out_conf.p, D.inv_per_px, cfg->subpixel_fit_points,
+                            cfg->subpixel_iterations, D.filled.p, nullptr, nullptr, C.stream));
+    unsigned int f = 0;
+    CK(cudaMemcpyAsync(depth->depth, D.out_depth.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(depth->confidence, D.out_conf.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(&f, D.filled.p, sizeof(f), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    if (out_refined) *out_refined = f;
+  });
+}
+
+RECON_API recon_status recon_mvs_geometric_consistency(const recon_mvs_depth_map* maps, const recon_pose* poses,
+                                                       const recon_camera_intrinsics* intr, int32_t num_maps,
+                                                       int32_t ref_index, float rel_depth_max, float reproj_px_max,
+                                                       int32_t min_views, uint8_t* out_count, uint8_t* out_keep) {
+  return guard([&] {
+    if (!maps || !poses || !intr || num_maps <= 0 || ref_index < 0 || ref_index >= num_maps || !out_count || !out_keep)
+      fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    Context& C = default_context(nullptr);
+    C.use();
+    std::vector<std::unique_ptr<DevArray<float>>> dev(num_maps);
+    for (int m = 0; m < num_maps; ++m) {
+      dev[m] = std::make_unique<DevArray<float>>();
+      if (!maps[m].depth) continue;
+      const size_t n = (size_t)maps[m].width * maps[m].height;
+      dev[m]->alloc(n);
+      CK(cudaMemcpyAsync(dev[m]->p, maps[m].depth, n * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+    }
+    const recon_mvs_depth_map& R = maps[ref_index];
+    if (!R.depth) fail(RECON_ERR_INVALID_ARGUMENT, "reference map NULL");
+    ConsistencyRef cr{R.width, R.height, dev[ref_index]->p, (float)intr[ref_index].fx, (float)intr[ref_index].fy,
+                      (float)intr[ref_index].cx, (float)intr[ref_index].cy};
+    std::vector<ConsistencySrc> srcs;
+    for (int s = 0; s < num_maps; ++s) {
+      if (s == ref_index || !maps[s].depth) continue;
+      ConsistencySrc cs;
+      std::memset(&cs, 0, sizeof(cs));
+      cs.w = maps[s].width;
+      cs.h = maps[s].height;
+      cs.depth = dev[s]->p;
+      cs.fx = (float)intr[s].fx;
+      cs.fy = (float)intr[s].fy;
+      cs.cx = (float)intr[s].cx;
+      cs.cy = (float)intr[s].cy;
+      double A[9], b[3], Ai[9], bi[3];
+      relative_transform(poses[ref_index], poses[s], A, b);
+      relative_transform(poses[s], poses[ref_index], Ai, bi);
+      for (int i = 0; i < 9; ++i) {
+        cs.A[i] = (float)A[i];
+        cs.Ai[i] = (float)Ai[i];
+      }
+      for (int i = 0; i < 3; ++i) {
+        cs.b[i] = (float)b[i];
+        cs.bi[i] = (float)bi[i];
+      }
+      srcs.push_back(cs);
+    }
+    DevArray<ConsistencySrc> ds;
+    ds.alloc(std::max<size_t>(1, srcs.size()));
+    if (!srcs.empty())
+      CK(cudaMemcpyAsync(ds.p, srcs.data(), srcs.size() * sizeof(ConsistencySrc), cudaMemcpyHostToDevice, C.stream));
+    const size_t n = (size_t)R.width * R.height;
+    DevArray<uint8_t> dc, dk;
+    dc.alloc(n);
+    dk.alloc(n);
+    CK(launch_consistency(cr, ds.p, (int)srcs.size(), rel_depth_max, reproj_px_max, min_views, dc.p, dk.p, C.stream));
+    CK(cudaMemcpyAsync(out_count, dc.p, n, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out_keep, dk.p, n, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+RECON_API void recon_mvs_point_cloud_free(recon_mvs_point_cloud* c) {
+  if (!c) return;
+  std::free(c->positions);
+  std::free(c->normals);
+  std::free(c->colors);
+  std::free(c->confidences);
+  std::free(c->keys);
+  std::free(c->counts);
+  std::memset(c, 0, sizeof(*c));
+}
+
+RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const recon_pose* poses,
+                                      const recon_camera_intrinsics* intr, int32_t num_maps,
+                                      const recon_mvs_config* cfg, const uint8_t* const* keep_masks,
+                                      recon_mvs_point_cloud* out) {
+  return guard([&] {
+    if (!out || !cfg) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    if (num_maps <= 0) return;
+    if (!maps || !poses || !intr) fail(RECON_ERR_INVALID_ARGUMENT, "NULL maps/poses/intrinsics");
+    if (cfg->fusion_voxel_size_m <= 0.0) return;
+    Context& C = default_context(nullptr);
+    C.use();
+    int64_t total = 0;
+    std::vector<int64_t> base(num_maps);
+    for (int m = 0; m < num_maps; ++m) {
+      base[m] = total;
+      if (maps[m].depth) total += (int64_t)maps[m].width * maps[m].height;
+    }
+    if (total == 0) return;
+    DevArray<unsigned long long> key, tkey, tfirst;
+    DevArray<double> pos, nrm;
+    DevArray<float> conf;
+    DevArray<uint8_t> valid;
+    DevArray<int> slot_of, err;
+    DevArray<unsigned int> tcount, flag, vid_of, slot_vid, scratch;
+    key.alloc(total);
+    pos.alloc(3 * total);
+    nrm.alloc(3 * total);
+    conf.alloc(total);
+    valid.alloc(total);
+    slot_of.alloc(total);
+    flag.alloc(total);
+    vid_of.alloc(total);
+    err.alloc(1);
+    uint64_t cap = 1024;
+    while (cap < 2 * (uint64_t)total) cap <<= 1;
+    tkey.alloc(cap);
+    tfirst.alloc(cap);
+    tcount.alloc(cap);
+    slot_vid.alloc(cap);
+    CK(cudaMemsetAsync(tkey.p, 0x7F, cap * sizeof(unsigned long long), C.stream));
+    CK(cudaMemsetAsync(tfirst.p, 0xFF, cap * sizeof(unsigned long long), C.stream));
+    CK(cudaMemsetAsync(tcount.p, 0, cap * sizeof(unsigned int), C.stream));
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), C.stream));
+    FuseParams P{cfg->fusion_voxel_size_m, cfg->photo_threshold, cfg->min_view_consistency};
+    std::vector<std::unique_ptr<DevArray<float>>> dd, dc;
+    std::vector<std::unique_ptr<DevArray<uint8_t>>> dsup, dkeep;
+    for (int m = 0; m < num_maps; ++m) {
+      if (!maps[m].depth) continue;
+      if (!maps[m].support_count || !maps[m].confidence) fail(RECON_ERR_INVALID_ARGUMENT, "map arrays NULL");
+      const size_t n = (size_t)maps[m].width * maps[m].height;
+      dd.push_back(std::make_unique<DevArray<float>>());
+      dc.push_back(std::make_unique<DevArray<float>>());
+      dsup.push_back(std::make_unique<DevArray<uint8_t>>());
+      dkeep.push_back(std::make_unique<DevArray<uint8_t>>());
+      dd.back()->alloc(n);
+      dc.back()->alloc(n);
+      dsup.back()->alloc(n);
+      CK(cudaMemcpyAsync(dd.back()->p, maps[m].depth, n * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+      CK(cudaMemcpyAsync(dc.back()->p, maps[m].confidence, n * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+      CK(cudaMemcpyAsync(dsup.back()->p, maps[m].support_count, n, cudaMemcpyHostToDevice, C.stream));
+      const uint8_t* keep = nullptr;
+      if (keep_masks && keep_masks[m]) {
+        dkeep.back()->alloc(n);
+        CK(cudaMemcpyAsync(dkeep.back()->p, keep_masks[m], n, cudaMemcpyHostToDevice, C.stream));
+        keep = dkeep.back()->p;
+      }
+      const recon_camera_intrinsics& k = intr[m];
+      FuseMap M;
+      std::memset(&M, 0, sizeof(M));
+      M.w = maps[m].width;
+      M.h = maps[m].height;
+      M.depth = dd.back()->p;
+      M.support = dsup.back()->p;
+      M.conf = dc.back()->p;
+      M.keep = keep;
+      M.fx = k.fx;
+      M.fy = k.fy;
+      M.cx = k.cx;
+      M.cy = k.cy;
+      M.k1 = k.k1;
+      M.k2 = k.k2;
+      M.k3 = k.k3;
+      M.p1 = k.p1;
+      M.p2 = k.p2;
+      for (int i = 0; i < 9; ++i) M.R[i] = poses[m].r[i];
+      for (int i = 0; i < 3; ++i) M.t[i] = poses[m].t[i];
+      CK(launch_fuse_points(M, base[m], P, key.p, pos.p, nrm.p, conf.p, valid.p, C.stream));
+    }
+    CK(launch_fuse_insert(total, key.p, valid.p, tkey.p, tcount.p, tfirst.p, cap - 1, slot_of.p, err.p, C.stream));
+    CK(launch_fuse_flags(total, valid.p, slot_of.p, tfirst.p, flag.p, C.stream));
+    scratch.alloc(scan_scratch_elems(total));
+    CK(exclusive_scan_u32(flag.p, vid_of.p, total, scratch.p, C.stream));
+    unsigned int last_vid = 0, last_flag = 0;
+    int herr = 0;
+    CK(cudaMemcpyAsync(&last_vid, vid_of.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(&last_flag, flag.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    if (herr) fail(RECON_ERR_INTERNAL, "voxel hash table overflow");
+    const unsigned int nvox = last_vid + last_flag;
+    if (nvox == 0) return;
+    DevArray<unsigned int> vcount, voffset, cursor;
+    vcount.alloc(nvox);
+    voffset.alloc(nvox);
+    cursor.alloc(nvox);
+    CK(launch_fuse_voxels(total, flag.p, vid_of.p, slot_of.p, tcount.p, slot_vid.p, vcount.p, C.stream));
+    scratch.alloc(std::max<int64_t>(scan_scratch_elems(nvox), (int64_t)scratch.n));
+    CK(exclusive_scan_u32(vcount.p, voffset.p, nvox, scratch.p, C.stream));
+    unsigned int last_off = 0, last_cnt = 0;
+    CK(cudaMemcpyAsync(&last_off, voffset.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(&last_cnt, vcount.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemsetAsync(cursor.p, 0, nvox * sizeof(unsigned int), C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    const int64_t npts = (int64_t)last_off + last_cnt;
+    DevArray<int64_t> bucket;
+    bucket.alloc(npts);
+    CK(launch_fuse_scatter(total, valid.p, slot_of.p, slot_vid.p, voffset.p, cursor.p, bucket.p, C.stream));
+    DevArray<unsigned long long> okey;
+    DevArray<double> opos, onrm;
+    DevArray<float> oconf;
+    DevArray<unsigned int> ocount;
+    okey.alloc(nvox);
+    opos.alloc(3 * (size_t)nvox);
+    onrm.alloc(3 * (size_t)nvox);
+    oconf.alloc(nvox);
+    ocount.alloc(nvox);
+    CK(launch_fuse_reduce(nvox, voffset.p, vcount.p, bucket.p, key.p, pos.p, nrm.p, conf.p, okey.p, opos.p, onrm.p,
+                          oconf.p, ocount.p, C.stream));
+    out->count = nvox;
+    out->positions = (double*)std::malloc(3 * sizeof(double) * nvox);
+    out->normals = (double*)std::malloc(3 * sizeof(double) * nvox);
+    out->colors = (float*)std::calloc(3 * (size_t)nvox, sizeof(float));
+    out->confidences = (float*)std::malloc(sizeof(float) * nvox);
+    out->keys = (int64_t*)std::malloc(sizeof(int64_t) * nvox);
+    out->counts = (uint32_t*)std::malloc(sizeof(uint32_t) * nvox);
+    if (!out->positions || !out->normals || !out->colors || !out->confidences || !out->keys || !out->counts) {
+      recon_mvs_point_cloud_free(out);
+      fail(RECON_ERR_OUT_OF_MEMORY, "point cloud allocation failed");
+    }
+    CK(cudaMemcpyAsync(out->positions, opos.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out->normals, onrm.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out->confidences, oconf.p, sizeof(float) * nvox, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out->keys, okey.p, sizeof(int64_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out->counts, ocount.p, sizeof(uint32_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+RECON_API recon_status recon_mvs_undistort(const uint8_t* img, int32_t w, int32_t h,
+                                           const recon_camera_intrinsics* intr, float* out) {
+  return guard([&] {
+    if (!img || !intr || !out || w <= 0 || h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    Context& C = default_context(nullptr);
+    C.use();
+    DevArray<uint8_t> di;
+    DevArray<float> dout;
+    di.alloc((size_t)w * h);
+    dout.alloc((size_t)w * h);
+    CK(cudaMemcpyAsync(di.p, img, (size_t)w * h, cudaMemcpyHostToDevice, C.stream));
+    UndistortCam K{intr->fx, intr->fy, intr->cx, intr->cy, intr->k1, intr->k2, intr->k3, intr->p1, intr->p2};
+    CK(launch_undistort(di.p, w, h, K, dout.p, C.stream));
+    CK(cudaMemcpyAsync(out, dout.p, (size_t)w * h * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+RECON_API recon_status recon_mvs_context_create(const recon_mvs_options* opts, void** out_ctx) {
+  return guard([&] {
+    if (!out_ctx) fail(RECON_ERR_INVALID_ARGUMENT, "out_ctx NULL");
+    recon_mvs_options o;
+    if (opts)
+      o = *opts;
+    else
+      fill_defaults(&o);
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (o.device < 0 || o.device >= ndev) fail(RECON_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    *out_ctx = new Context(o);
+  });
+}
+
+RECON_API void recon_mvs_context_destroy(void* ctx) { delete static_cast<Context*>(ctx); }
+
+RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* views, const recon_mvs_config* cfg,
+                                           int32_t undistort, int32_t* out_job) {
+  return guard([&] {
+    if (!ctx || !out_job) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out_job = stage_job(*static_cast<Context*>(ctx), views, cfg, undistort != 0, nullptr, 0);
+  });
+}
+
+RECON_API recon_status recon_mvs_job_run(void* ctx, int32_t job) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    run_job(C, get_job(C, job));
+  });
+}
+
+RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_t n) {
+  return guard([&] {
+    if (!ctx || (!jobs && n > 0)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    Context& C = *static_cast<Context*>(ctx);
+    for (int i = 0; i < n; ++i) run_job(C, get_job(C, jobs[i]));
+  });
+}
+
+RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out, uint32_t* filled) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    download_job(C, get_job(C, job), out, filled);
+  });
+}
+
+RECON_API recon_status recon_mvs_job_release(void* ctx, int32_t job) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    CK(cudaStreamSynchronize(C.stream));
+    if (!C.jobs.erase(job)) fail(RECON_ERR_INVALID_ARGUMENT, "unknown job id");
+  });
+}
+
+RECON_API recon_status recon_mvs_synchronize(void* ctx) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    CK(cudaStreamSynchronize(C.stream));
+    finish_stats(C);
+  });
+}
+
+RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out) {
+  return guard([&] {
+    if (!ctx || !out) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    unsigned long long ev = 0;
+    CK(cudaMemcpy(&ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
+    C.stats.hypotheses_evaluated = ev;
+    *out = C.stats;
+  });
+}
+
+}  // extern "C"

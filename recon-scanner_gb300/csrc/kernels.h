@@ -1,0 +1,105 @@
+// kernels.h -- launch interface between the host runtime (engine.cu) and
+// the kernels (pm.cu, fusion.cu).  Internal to the library.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace rmvs {
+
+// ---- fusion / consistency / undistortion descriptors ----
+struct FuseMap {
+  int w, h;
+  const float* depth;
+  const uint8_t* support;
+  const float* conf;
+  const uint8_t* keep;  // optional consistency mask
+  double fx, fy, cx, cy, k1, k2, k3, p1, p2;
+  double R[9], t[3];
+};
+
+struct FuseParams {
+  double voxel;
+  double photo_threshold;
+  int min_view_consistency;
+};
+
+struct ConsistencyRef {
+  int w, h;
+  const float* depth;
+  float fx, fy, cx, cy;
+};
+
+struct ConsistencySrc {
+  int w, h;
+  const float* depth;
+  float fx, fy, cx, cy;
+  float A[9], b[3];    // reference camera -> this camera
+  float Ai[9], bi[3];  // this camera -> reference camera
+};
+
+struct UndistortCam {
+  double fx, fy, cx, cy, k1, k2, k3, p1, p2;
+};
+
+struct NccWindow {
+  double ref_u, ref_v, src_u, src_v;
+};
+
+// ---- PatchMatch ----
+cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const int* py, const double* inv,
+                             const float* normals, float* cost, int* support, float* view_cost, cudaStream_t st);
+cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st);
+cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters, cudaStream_t st);
+cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st);
+cudaError_t launch_plane_output(const Job& J, float* depth, uint8_t* support, float* conf, float* normal, float* cost,
+                                unsigned int* filled, cudaStream_t st);
+cudaError_t launch_compat_init(const Job& J, float* cost, cudaStream_t st);
+cudaError_t launch_compat_sweep(const Job& J, const double* inv_in, const float* cost_in, const int32_t* sup_in,
+                                double* inv_out, float* cost_out, int32_t* sup_out, const uint32_t* draws,
+                                const uint8_t* fire, int draw_stride, int search_count, double radius_ratio,
+                                int propagate, cudaStream_t st);
+cudaError_t launch_compat_output(const Job& J, const double* inv, const float* cost, const int32_t* sup, float* depth,
+                                 uint8_t* support, float* conf, unsigned int* filled, cudaStream_t st);
+cudaError_t launch_compat_refine(const Job& J, float* depth, float* conf, double inv_per_px, int fit_points, int iters,
+                                 unsigned int* refined, double* best_inv, float* best_cost, cudaStream_t st);
+cudaError_t launch_prep_ref(const uint8_t* img, int w, int h, float* ref, float* box, cudaStream_t st);
+cudaError_t launch_prep_ref_f32(const float* img, int w, int h, float* ref, float* box, cudaStream_t st);
+cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+                            cudaStream_t st);
+cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+                                  cudaStream_t st);
+cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);
+cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,
+                               int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,
+                               int* samples, cudaStream_t st);
+
+// ---- fusion ----
+cudaError_t launch_fuse_points(const FuseMap& M, int64_t base, const FuseParams& P, unsigned long long* key,
+                               double* pos, double* nrm, float* conf, uint8_t* valid, cudaStream_t st);
+cudaError_t launch_fuse_insert(int64_t n, const unsigned long long* key, const uint8_t* valid,
+                               unsigned long long* tkey, unsigned int* tcount, unsigned long long* tfirst,
+                               uint64_t mask, int* slot_of, int* error, cudaStream_t st);
+cudaError_t launch_fuse_flags(int64_t n, const uint8_t* valid, const int* slot_of, const unsigned long long* tfirst,
+                              unsigned int* flag, cudaStream_t st);
+cudaError_t launch_fuse_voxels(int64_t n, const unsigned int* flag, const unsigned int* vid_of, const int* slot_of,
+                               const unsigned int* tcount, unsigned int* slot_vid, unsigned int* vcount,
+                               cudaStream_t st);
+cudaError_t launch_fuse_scatter(int64_t n, const uint8_t* valid, const int* slot_of, const unsigned int* slot_vid,
+                                const unsigned int* voffset, unsigned int* cursor, int64_t* bucket, cudaStream_t st);
+cudaError_t launch_fuse_reduce(unsigned int nvox, const unsigned int* voffset, const unsigned int* vcount,
+                               int64_t* bucket, const unsigned long long* key, const double* pos, const double* nrm,
+                               const float* conf, unsigned long long* okey, double* opos, double* onrm, float* oconf,
+                               unsigned int* ocount, cudaStream_t st);
+cudaError_t launch_consistency(const ConsistencyRef& R, const ConsistencySrc* S, int num_src, float rel_max,
+                               float reproj_px_max, int min_views, uint8_t* count, uint8_t* keep, cudaStream_t st);
+cudaError_t launch_undistort(const uint8_t* img, int w, int h, const UndistortCam& K, float* out, cudaStream_t st);
+
+int64_t scan_scratch_elems(int64_t n);
+cudaError_t exclusive_scan_u32(const unsigned int* in, unsigned int* out, int64_t n, unsigned int* scratch,
+                               cudaStream_t st);
+
+}  // namespace rmvs

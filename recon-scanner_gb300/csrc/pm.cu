@@ -1,0 +1,962 @@
+// pm.cu -- PatchMatch kernels: hypothesis evaluation, plane-mode red-black
+// sweeps, compat-mode (reference) Jacobi sweeps, outputs, refinement.
+//
+// Plane mode (the GB300 engine): per-pixel plane hypotheses (inverse depth,
+// normal), red-black checkerboard propagation -- a half-sweep updates one
+// colour reading only the other colour, so it is race-free and
+// deterministic -- with adaptive neighbour selection (best cost in each of 8
+// regions) and random perturbation; cost = mean of the best_k view costs.
+//
+// Compat mode (drop-in parity): the reference PatchMatchStereo exactly --
+// fronto-parallel inverse-depth hypotheses, translated windows, and the
+// reference's Jacobi sweeps (every pixel reads the sweep's snapshot,
+// patchmatch_stereo.cpp:615-740), run one thread per pixel; the reference's
+// row-block xorshift draws are generated on the host in its scan order.
+#include <cuda_fp16.h>
+
+#include <cstdio>
+
+#include "cost.cuh"
+#include "kernels.h"
+
+namespace rmvs {
+
+// ---------------------------------------------------------------------------
+// per-thread source-ray cache in shared memory: P[s][c] as float2 (hi, lo)
+// ---------------------------------------------------------------------------
+struct PCache {
+  float2* base;
+  int stride;  // threads per block
+  int tid;
+  __device__ __forceinline__ void get(int s, ff P[3]) const {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 v = base[(s * 3 + c) * stride + tid];
+      P[c] = ff{v.x, v.y};
+    }
+  }
+  __device__ __forceinline__ void put(int s, const ff P[3]) const {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) base[(s * 3 + c) * stride + tid] = make_float2(P[c].hi, P[c].lo);
+  }
+};
+
+__device__ __forceinline__ void fill_pcache(const Job& J, const PCache& pc, int x, int y, float* rx, float* ry) {
+  double ray[3];
+  ref_ray(J, x + 0.5, y + 0.5, ray);
+  for (int s = 0; s < J.num_src; ++s) {
+    ff P[3];
+    source_rays(J, J.src[s], ray, P);
+    pc.put(s, P);
+  }
+  *rx = (float)ray[0];
+  *ry = (float)ray[1];
+}
+
+// ---------------------------------------------------------------------------
+// full hypothesis evaluation over all sources
+// ---------------------------------------------------------------------------
+struct HypCost {
+  float cost;
+  int support;
+};
+
+constexpr int kMaxBestK = 8;
+
+__device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int nvalid, int best_k,
+                                                float photo_threshold) {
+  HypCost r{kCostInf, nvalid};
+  if (nvalid == 0) return r;
+  float c;
+  if (best_k <= 0 || best_k >= nvalid || best_k > kMaxBestK) {
+    c = sum_all / (float)nvalid;
+  } else {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < kMaxBestK; ++i)
+      if (i < best_k) s += best[i];
+    c = s / (float)best_k;
+  }
+  if (c > 3.0f * photo_threshold) c = kCostInf;
+  r.cost = c;
+  return r;
+}
+
+__device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
+                                  float nx, float ny, float nz, const RefWindow& rw, float* view_cost,
+                                  int* nevals = nullptr) {
+  HypCost bad{kCostInf, 0};
+  if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max) return bad;
+  PlaneHyp hp;
+  if (!make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) return bad;
+  if (nevals) ++*nevals;
+  float best[kMaxBestK];
+#pragma unroll
+  for (int i = 0; i < kMaxBestK; ++i) best[i] = kCostInf;
+  float sum_all = 0.f;
+  int nvalid = 0;
+  for (int s = 0; s < J.num_src; ++s) {
+    ff P[3];
+    pc.get(s, P);
+    const ViewResult v = eval_view_plane(J, J.src[s], x, y, P, hp, rw);
+    float c = kCostInf;
+    if (v.valid) {
+      c = 1.0f - v.ncc;
+      ++nvalid;
+      sum_all += c;
+#pragma unroll
+      for (int i = 0; i < kMaxBestK; ++i) {
+        const float lo = fminf(best[i], c), hi = fmaxf(best[i], c);
+        best[i] = lo;
+        c = hi;
+      }
+      c = 1.0f - v.ncc;
+    }
+    if (view_cost) view_cost[s] = c;
+  }
+  return finish_plane(best, sum_all, nvalid, J.best_k, J.photo_threshold);
+}
+
+// COMPAT: 1 - mean NCC over valid views (patchmatch_stereo.cpp:344-418).
+__device__ HypCost eval_compat_hyp(const Job& J, const PCache& pc, int x, int y, double inv, const RefWindow& rw,
+                                   float* view_cost) {
+  HypCost bad{kCostInf, 0};
+  if (inv <= 1e-9) return bad;
+  const double depth = 1.0 / inv;
+  if (depth < J.min_depth || depth > J.max_depth) return bad;
+  const float hi = (float)inv;
+  const ff rho{hi, (float)(inv - (double)hi)};
+  float sum = 0.f;
+  int nvalid = 0;
+  for (int s = 0; s < J.num_src; ++s) {
+    ff P[3];
+    pc.get(s, P);
+    const ViewResult v = eval_view_compat(J, J.src[s], x, y, P, rho, hi, rw);
+    if (v.valid) {
+      ++nvalid;
+      sum += v.ncc;
+    }
+    if (view_cost) view_cost[s] = v.valid ? 1.0f - v.ncc : kCostInf;
+  }
+  HypCost r{kCostInf, nvalid};
+  if (nvalid == 0) return r;
+  float c = 1.0f - sum / (float)nvalid;
+  if (c > 3.0f * J.photo_threshold) c = kCostInf;
+  r.cost = c;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// batch evaluation of given hypotheses (parity instrument, adjoint driver)
+// ---------------------------------------------------------------------------
+__global__ void k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
+                            const double* __restrict__ inv, const float* __restrict__ normals, float* out_cost,
+                            int* out_support, float* out_view_cost) {
+  extern __shared__ float2 smem[];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)blockDim.x, (int)threadIdx.x};
+  if (i >= n) return;
+  const int x = px[i], y = py[i];
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  float* vc = out_view_cost ? out_view_cost + (size_t)i * J.num_src : nullptr;
+  HypCost r;
+  if (mode == 0) {
+    const RefWindow rw = ref_window(J, x, y, true);
+    r = eval_compat_hyp(J, pc, x, y, inv[i], rw, vc);
+  } else {
+    const RefWindow rw = ref_window(J, x, y, false);
+    r = eval_plane_hyp(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
+                       rw, vc);
+  }
+  out_cost[i] = r.cost;
+  out_support[i] = r.support;
+}
+
+// ---------------------------------------------------------------------------
+// plane mode
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void random_normal(Rng& g, float rx, float ry, float* nx, float* ny, float* nz) {
+  // uniform direction, flipped to face the camera, kept off grazing angles
+  const float rn = rsqrtf(rx * rx + ry * ry + 1.0f);
+  for (int t = 0; t < 8; ++t) {
+    const float z = g.sym();
+    const float phi = 6.28318530718f * g.uniform();
+    const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float a = r * __cosf(phi), b = r * __sinf(phi), c = z;
+    float d = (a * rx + b * ry + c) * rn;
+    if (d > 0.f) {
+      a = -a;
+      b = -b;
+      c = -c;
+      d = -d;
+    }
+    if (d < -0.2f) {
+      *nx = a;
+      *ny = b;
+      *nz = c;
+      return;
+    }
+  }
+  *nx = 0.f;
+  *ny = 0.f;
+  *nz = -1.f;
+}
+
+__device__ __forceinline__ void perturb_normal(Rng& g, float rx, float ry, float scale, float* nx, float* ny,
+                                               float* nz) {
+  float a = *nx + scale * g.sym(), b = *ny + scale * g.sym(), c = *nz + scale * g.sym();
+  const float inv = rsqrtf(a * a + b * b + c * c);
+  a *= inv;
+  b *= inv;
+  c *= inv;
+  const float rn = rsqrtf(rx * rx + ry * ry + 1.0f);
+  if ((a * rx + b * ry + c) * rn < -0.2f) {
+    *nx = a;
+    *ny = b;
+    *nz = c;
+  }
+}
+
+__device__ __forceinline__ Rng pixel_rng(const Job& J, int idx, int iter, int salt) {
+  Rng g;
+  g.s = mix64(J.seed ^ ((uint64_t)idx * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(iter + 1) << 40) ^
+              ((uint64_t)salt << 56));
+  return g;
+}
+
+__global__ void k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
+  extern __shared__ float2 smem[];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  Rng g = pixel_rng(J, idx, -1, 1);
+  float rho = J.rho_min + (J.rho_max - J.rho_min) * g.uniform();
+  float nx, ny, nz;
+  random_normal(g, rx, ry, &nx, &ny, &nz);
+  if (seed_depth) {
+    const int cx = min(x / seed_grid, seed_gx - 1);
+    const int cy = y / seed_grid;
+    const float sd = seed_depth[cy * seed_gx + cx];
+    if (sd > 0.f) {
+      rho = 1.0f / sd;
+      nx = 0.f;
+      ny = 0.f;
+      nz = -1.f;
+    }
+  }
+  const RefWindow rw = ref_window(J, x, y, false);
+  const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, nullptr);
+  J.hyp[idx] = make_float4(rho, nx, ny, nz);
+  J.cost[idx] = c.cost;
+  J.support[idx] = (uint8_t)min(c.support, 255);
+}
+
+// Adaptive checkerboard regions (other-colour pixels only: dx + dy odd).
+// 4 near "V" regions of 7 pixels and 4 far strips of 11 pixels.
+__constant__ signed char c_near[4][7][2] = {
+    {{0, -1}, {-1, -2}, {1, -2}, {-2, -3}, {2, -3}, {-3, -4}, {3, -4}},
+    {{0, 1}, {-1, 2}, {1, 2}, {-2, 3}, {2, 3}, {-3, 4}, {3, 4}},
+    {{-1, 0}, {-2, -1}, {-2, 1}, {-3, -2}, {-3, 2}, {-4, -3}, {-4, 3}},
+    {{1, 0}, {2, -1}, {2, 1}, {3, -2}, {3, 2}, {4, -3}, {4, 3}}};
+
+__device__ __forceinline__ void plane_candidate_transfer(const float4 hn, float rxn, float ryn, float rx, float ry,
+                                                         float* rho) {
+  // the neighbour's plane n . X = kappa_n / rho_n, evaluated on this pixel's ray
+  const float kn = hn.y * rxn + hn.z * ryn + hn.w;
+  const float kp = hn.y * rx + hn.z * ry + hn.w;
+  *rho = (kn < 0.f && kp < 0.f) ? hn.x * kp / kn : -1.0f;
+}
+
+__global__ void __launch_bounds__(128) k_plane_sweep(Job J, int color, int iter, int num_iters) {
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int x = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + ((y + color) & 1);
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, false);
+  float4 cur = J.hyp[idx];
+  float cur_cost = J.cost[idx];
+  int cur_sup = J.support[idx];
+  const float ifx = 1.0f / J.rfx, ify = 1.0f / J.rfy;
+  int nevals = 0;
+
+  // --- propagation: best-cost neighbour of each region ---
+  for (int r = 0; r < 8; ++r) {
+    int best_n = -1;
+    float best_c = kCostInf;
+    if (r < 4) {
+      for (int k = 0; k < 7; ++k) {
+        const int nx_ = x + c_near[r][k][0], ny_ = y + c_near[r][k][1];
+        if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
+        const float c = J.cost[ny_ * J.w + nx_];
+        if (c < best_c) {
+          best_c = c;
+          best_n = ny_ * J.w + nx_;
+        }
+      }
+    } else {
+      const int d = r - 4;
+      const int sx = d == 2 ? -1 : (d == 3 ? 1 : 0);
+      const int sy = d == 0 ? -1 : (d == 1 ? 1 : 0);
+      for (int k = 0; k < 11; ++k) {
+        const int off = 3 + 2 * k;
+        const int nx_ = x + sx * off, ny_ = y + sy * off;
+        if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
+        const float c = J.cost[ny_ * J.w + nx_];
+        if (c < best_c) {
+          best_c = c;
+          best_n = ny_ * J.w + nx_;
+        }
+      }
+    }
+    if (best_n < 0 || best_c >= kCostInf) continue;
+    const float4 hn = J.hyp[best_n];
+    const int nxp = best_n % J.w, nyp = best_n / J.w;
+    float rho;
+    plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
+    if (!(rho > 0.f)) continue;
+    if (rho == cur.x && hn.y == cur.y && hn.z == cur.z && hn.w == cur.w) continue;
+    const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, nullptr, &nevals);
+    if (c.cost < cur_cost) {
+      cur_cost = c.cost;
+      cur = make_float4(rho, hn.y, hn.z, hn.w);
+      cur_sup = c.support;
+    }
+  }
+
+  // --- refinement: random and perturbed hypotheses, shrinking with iterations ---
+  Rng g = pixel_rng(J, idx, iter, 2 + color);
+  const float scale = exp2f(-(float)iter);  // 1, 1/2, 1/4, ...
+  const float span = J.rho_max - J.rho_min;
+  for (int k = 0; k < 4; ++k) {
+    float rho = cur.x, nx = cur.y, ny = cur.z, nz = cur.w;
+    if (k == 0) {
+      rho = J.rho_min + span * g.uniform();
+      random_normal(g, rx, ry, &nx, &ny, &nz);
+    } else {
+      if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
+      if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
+    }
+    const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, nullptr, &nevals);
+    if (c.cost < cur_cost) {
+      cur_cost = c.cost;
+      cur = make_float4(rho, nx, ny, nz);
+      cur_sup = c.support;
+    }
+  }
+  if (J.eval_counter) {
+    const unsigned int lane_sum = __reduce_add_sync(__activemask(), (unsigned int)nevals);
+    if ((threadIdx.x & 31) == (__ffs(__activemask()) - 1)) atomicAdd(J.eval_counter, (unsigned long long)lane_sum);
+  }
+  J.hyp[idx] = cur;
+  J.cost[idx] = cur_cost;
+  J.support[idx] = (uint8_t)min(cur_sup, 255);
+}
+
+__global__ void k_plane_output(Job J, float* depth, uint8_t* support, float* conf, float* normal, float* cost_out,
+                               unsigned int* filled) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  const float4 h = J.hyp[idx];
+  const float c = J.cost[idx];
+  float d = __int_as_float(0x7fc00000);
+  float cf = 0.f;
+  uint8_t sp = 0;
+  if (c < 1e29f && h.x > 0.f) {
+    const float dd = 1.0f / h.x;
+    if (dd >= (float)J.min_depth && dd <= (float)J.max_depth) {
+      d = dd;
+      cf = 1.0f - fminf(1.0f, fmaxf(0.0f, c));
+      sp = J.support[idx];
+      atomicAdd(filled, 1u);
+    }
+  }
+  depth[idx] = d;
+  support[idx] = sp;
+  conf[idx] = cf;
+  if (normal) {
+    normal[3 * idx] = h.y;
+    normal[3 * idx + 1] = h.z;
+    normal[3 * idx + 2] = h.w;
+  }
+  if (cost_out) cost_out[idx] = c;
+}
+
+// ---------------------------------------------------------------------------
+// compat mode (the reference algorithm)
+// ---------------------------------------------------------------------------
+__global__ void k_compat_init(Job J, float* cost) {
+  extern __shared__ float2 smem[];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, true);
+  const HypCost c = eval_compat_hyp(J, pc, x, y, J.inv[idx], rw, nullptr);
+  cost[idx] = c.cost;
+  J.isupport[idx] = c.support;
+}
+
+// One direction sweep (patchmatch_stereo.cpp:642-723) for every pixel at
+// once: candidates come from the snapshot (inv_in, cost_in); the pixel's own
+// draws -- random_search_count signed draws, the restart flag and the
+// restart draw -- were generated on the host in the reference's scan order.
+__global__ void k_compat_sweep(Job J, const double* __restrict__ inv_in, const float* __restrict__ cost_in,
+                               const int32_t* __restrict__ sup_in, double* inv_out, float* cost_out,
+                               int32_t* sup_out, const uint32_t* __restrict__ draws, const uint8_t* __restrict__ fire,
+                               int draw_stride, int search_count, double radius_ratio, int propagate) {
+  extern __shared__ float2 smem[];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, true);
+  double out_inv = inv_in[idx];
+  float out_cost = cost_in[idx];
+  int out_sup = sup_in[idx];
+  if (propagate) {
+    const int nbx[4] = {-1, 1, 0, 0}, nby[4] = {0, 0, -1, 1};
+    for (int k = 0; k < 4; ++k) {
+      const int nx_ = x + nbx[k], ny_ = y + nby[k];
+      if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
+      const int n = ny_ * J.w + nx_;
+      if (cost_in[n] >= 1e29f) continue;
+      const double cand = inv_in[n];
+      const HypCost c = eval_compat_hyp(J, pc, x, y, cand, rw, nullptr);
+      if (c.cost < out_cost) {
+        out_cost = c.cost;
+        out_inv = cand;
+        out_sup = c.support;
+      }
+    }
+  }
+  const uint32_t* d = draws + (size_t)idx * draw_stride;
+  double radius = out_inv * radius_ratio;
+  for (int k = 0; k < search_count; ++k) {
+    const double sgn = ((double)d[k] / 4294967296.0) * 2.0 - 1.0;
+    const double cand = out_inv + sgn * radius;
+    if (cand < J.dinv_min || cand > J.dinv_max) {
+      radius *= 0.5;
+      continue;
+    }
+    const HypCost c = eval_compat_hyp(J, pc, x, y, cand, rw, nullptr);
+    if (c.cost < out_cost) {
+      out_cost = c.cost;
+      out_inv = cand;
+      out_sup = c.support;
+    }
+    radius *= 0.5;
+  }
+  if (fire[idx]) {
+    const double cand = J.dinv_min + ((double)d[search_count] / 4294967296.0) * (J.dinv_max - J.dinv_min);
+    const HypCost c = eval_compat_hyp(J, pc, x, y, cand, rw, nullptr);
+    if (c.cost < out_cost) {
+      out_cost = c.cost;
+      out_inv = cand;
+      out_sup = c.support;
+    }
+  }
+  inv_out[idx] = out_inv;
+  cost_out[idx] = out_cost;
+  sup_out[idx] = out_sup;
+}
+
+// patchmatch_stereo.cpp:744-763
+__global__ void k_compat_output(Job J, const double* __restrict__ inv, const float* __restrict__ cost,
+                                const int32_t* __restrict__ sup, float* depth, uint8_t* support, float* conf,
+                                unsigned int* filled) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  float d = __int_as_float(0x7fc00000);
+  float cf = 0.f;
+  uint8_t sp = 0;
+  if (cost[idx] < 1e29f) {
+    const double iv = inv[idx];
+    const double dd = iv <= 1e-9 ? 1e9 : 1.0 / iv;
+    if (!(dd < J.min_depth || dd > J.max_depth)) {
+      d = (float)dd;
+      sp = (uint8_t)min(sup[idx], 255);
+      const double pc = fmin(1.0, fmax(0.0, (double)cost[idx]));
+      cf = (float)(1.0 - pc);
+      atomicAdd(filled, 1u);
+    }
+  }
+  depth[idx] = d;
+  support[idx] = sp;
+  conf[idx] = cf;
+}
+
+// RefineSubpixel (patchmatch_stereo.cpp:770-979), one thread per pixel.
+// Inverse-depth arithmetic in FP64 as in the reference; costs FP32.
+__device__ __forceinline__ bool solve3(const double A[3][3], const double b[3], double x[3]) {
+  double m[3][4];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) m[i][j] = A[i][j];
+    m[i][3] = b[i];
+  }
+  for (int col = 0; col < 3; ++col) {
+    int pivot = col;
+    for (int r = col + 1; r < 3; ++r)
+      if (fabs(m[r][col]) > fabs(m[pivot][col])) pivot = r;
+    if (fabs(m[pivot][col]) < 1e-18) return false;
+    if (pivot != col)
+      for (int j = 0; j < 4; ++j) {
+        const double t = m[col][j];
+        m[col][j] = m[pivot][j];
+        m[pivot][j] = t;
+      }
+    for (int r = 0; r < 3; ++r) {
+      if (r == col) continue;
+      const double f = m[r][col] / m[col][col];
+      for (int j = col; j < 4; ++j) m[r][j] -= f * m[col][j];
+    }
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (fabs(m[i][i]) < 1e-18) return false;
+    x[i] = m[i][3] / m[i][i];
+  }
+  return true;
+}
+
+__global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per_px, int fit_points_cfg,
+                                int subpixel_iterations, unsigned int* refined, double* out_best_inv,
+                                float* out_best_cost) {
+  extern __shared__ float2 smem[];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  const float d0 = depth[idx];
+  if (out_best_inv) {
+    out_best_inv[idx] = __longlong_as_double(0x7ff8000000000000ll);
+    out_best_cost[idx] = kCostInf;
+  }
+  if (!isfinite(d0)) return;
+  const double inv0 = (double)d0 < 1e-9 ? 1e9 : 1.0 / (double)d0;
+  if (inv0 < J.dinv_min || inv0 > J.dinv_max) return;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, true);
+  auto eval = [&](double v) -> float { return eval_compat_hyp(J, pc, x, y, v, rw, nullptr).cost; };
+  const int fit_points = fit_points_cfg > 3 ? fit_points_cfg : 3;
+  const int half_fit = fit_points / 2;
+  const double fit_step = inv_per_px * 0.5;
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, t0 = 0, t1 = 0, t2 = 0;
+  bool fit_ok = fit_points <= 64;
+  for (int k = 0; k < fit_points && fit_ok; ++k) {
+    const double dk = inv0 + (k - half_fit) * fit_step;
+    if (dk < J.dinv_min || dk > J.dinv_max) {
+      fit_ok = false;
+      break;
+    }
+    const double c = (double)eval(dk);
+    if (c >= 1e29) fit_ok = false;
+    const double xx = (double)(k - half_fit);
+    s0 += 1.0;
+    s1 += xx;
+    s2 += xx * xx;
+    s3 += xx * xx * xx;
+    s4 += xx * xx * xx * xx;
+    t0 += c;
+    t1 += xx * c;
+    t2 += xx * xx * c;
+  }
+  double best_d = inv0;
+  float best_c = eval(inv0);
+  if (fit_ok) {
+    const double A[3][3] = {{s4, s3, s2}, {s3, s2, s1}, {s2, s1, s0}};
+    const double b[3] = {t2, t1, t0};
+    double sol[3];
+    if (solve3(A, b, sol) && fabs(sol[0]) > 1e-12) {
+      const double vertex = -sol[1] / (2.0 * sol[0]);
+      // the vertex is in sample-index units and is added unscaled, as in
+      // the reference (patchmatch_stereo.cpp:896-899)
+      if (vertex >= -(double)half_fit && vertex <= (double)half_fit) {
+        const double cand = inv0 + vertex;
+        const float cc = eval(cand);
+        if (cc < best_c) {
+          best_c = cc;
+          best_d = cand;
+        }
+      }
+    }
+  }
+  {
+    double lo = best_d - inv_per_px * 1.0;
+    double hi = best_d + inv_per_px * 1.0;
+    if (lo < J.dinv_min) lo = J.dinv_min;
+    if (hi > J.dinv_max) hi = J.dinv_max;
+    if (hi > lo) {
+      const double inv_phi = 0.6180339887498949;
+      double c1 = hi - inv_phi * (hi - lo);
+      double c2 = lo + inv_phi * (hi - lo);
+      float f1 = eval(c1), f2 = eval(c2);
+      for (int k = 0; k < subpixel_iterations; ++k) {
+        if (f1 < f2) {
+          hi = c2;
+          c2 = c1;
+          f2 = f1;
+          c1 = hi - inv_phi * (hi - lo);
+          f1 = eval(c1);
+        } else {
+          lo = c1;
+          c1 = c2;
+          f1 = f2;
+          c2 = lo + inv_phi * (hi - lo);
+          f2 = eval(c2);
+        }
+      }
+      const double mid = 0.5 * (lo + hi);
+      const float cm = eval(mid);
+      if (cm < best_c) {
+        best_c = cm;
+        best_d = mid;
+      }
+      if (f1 < best_c) {
+        best_c = f1;
+        best_d = c1;
+      }
+      if (f2 < best_c) {
+        best_c = f2;
+        best_d = c2;
+      }
+    }
+  }
+  if (out_best_inv) {
+    out_best_inv[idx] = best_d;
+    out_best_cost[idx] = best_c;
+  }
+  if (best_d < J.dinv_min || best_d > J.dinv_max) return;
+  const double fd = best_d <= 1e-9 ? 1e9 : 1.0 / best_d;
+  if (fd < J.min_depth || fd > J.max_depth) return;
+  depth[idx] = (float)fd;
+  const double pcost = fmin(1.0, fmax(0.0, (double)best_c));
+  conf[idx] = (float)(1.0 - pcost);
+  atomicAdd(refined, 1u);
+}
+
+// Plane-mode refinement: golden-section search on the inverse depth along
+// the pixel's own plane normal over +-1 px of disparity, the reference's
+// refinement schedule applied to the plane cost.
+__global__ void k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
+  extern __shared__ float2 smem[];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
+  if (x >= J.w || y >= J.h) return;
+  const int idx = y * J.w + x;
+  const float4 h0 = J.hyp[idx];
+  const float c0 = J.cost[idx];
+  if (!(c0 < 1e29f)) return;
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, false);
+  auto eval = [&](float v) -> HypCost { return eval_plane_hyp(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, nullptr); };
+  float best_d = h0.x, best_c = c0;
+  int best_s = J.support[idx];
+  float lo = fmaxf(J.rho_min, best_d - (float)inv_per_px);
+  float hi = fminf(J.rho_max, best_d + (float)inv_per_px);
+  if (hi > lo) {
+    const float inv_phi = 0.618033988749895f;
+    float c1 = hi - inv_phi * (hi - lo), c2 = lo + inv_phi * (hi - lo);
+    HypCost f1 = eval(c1), f2 = eval(c2);
+    for (int k = 0; k < subpixel_iterations; ++k) {
+      if (f1.cost < f2.cost) {
+        hi = c2;
+        c2 = c1;
+        f2 = f1;
+        c1 = hi - inv_phi * (hi - lo);
+        f1 = eval(c1);
+      } else {
+        lo = c1;
+        c1 = c2;
+        f1 = f2;
+        c2 = lo + inv_phi * (hi - lo);
+        f2 = eval(c2);
+      }
+    }
+    const float mid = 0.5f * (lo + hi);
+    const HypCost fm = eval(mid);
+    if (fm.cost < best_c) {
+      best_c = fm.cost;
+      best_d = mid;
+      best_s = fm.support;
+    }
+    if (f1.cost < best_c) {
+      best_c = f1.cost;
+      best_d = c1;
+      best_s = f1.support;
+    }
+    if (f2.cost < best_c) {
+      best_c = f2.cost;
+      best_d = c2;
+      best_s = f2.support;
+    }
+  }
+  J.hyp[idx] = make_float4(best_d, h0.y, h0.z, h0.w);
+  J.cost[idx] = best_c;
+  J.support[idx] = (uint8_t)min(best_s, 255);
+}
+
+// ---------------------------------------------------------------------------
+// image preparation
+// ---------------------------------------------------------------------------
+__global__ void k_prep_ref(const uint8_t* __restrict__ img, int w, int h, float* ref, float* box) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float v = (float)img[y * w + x] - 128.0f;
+  ref[y * w + x] = v;
+  if (box) {
+    // the reference's window sample at (x + 0.5, y + 0.5): an exact 2x2
+    // average; defined for x <= w-2, y <= h-2 (SampleBilinear's range)
+    const int x1 = min(x + 1, w - 1), y1 = min(y + 1, h - 1);
+    const float s = (float)img[y * w + x] + (float)img[y * w + x1] + (float)img[y1 * w + x] + (float)img[y1 * w + x1];
+    box[y * w + x] = 0.25f * s - 128.0f;
+  }
+}
+
+__global__ void k_prep_src_f32(const uint8_t* __restrict__ img, int w, int h, float* out, size_t pitch_elems) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  out[y * pitch_elems + x] = (float)img[y * w + x] - 128.0f;
+}
+
+__global__ void k_prep_src_f16(const uint8_t* __restrict__ img, int w, int h, __half* out, size_t pitch_elems) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  out[y * pitch_elems + x] = __float2half_rn((float)img[y * w + x] - 128.0f);
+}
+
+__global__ void k_prep_ref_f32(const float* __restrict__ img, int w, int h, float* ref, float* box) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  ref[y * w + x] = img[y * w + x] - 128.0f;
+  if (box) {
+    const int x1 = min(x + 1, w - 1), y1 = min(y + 1, h - 1);
+    const float s = (img[y * w + x] + img[y * w + x1]) + (img[y1 * w + x] + img[y1 * w + x1]);
+    box[y * w + x] = 0.25f * s - 128.0f;
+  }
+}
+
+__global__ void k_prep_src_f32in(const float* __restrict__ img, int w, int h, void* out, size_t pitch_elems, int fp16) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float v = img[y * w + x] - 128.0f;
+  if (fp16)
+    ((__half*)out)[y * pitch_elems + x] = __float2half_rn(v);
+  else
+    ((float*)out)[y * pitch_elems + x] = v;
+}
+
+// ComputeNcc (patchmatch_stereo.cpp:214-274) for a batch of windows, FP64 in
+// the reference's operation order: a standalone API, not the hot path.
+__device__ __forceinline__ bool sample_bilinear_d(const uint8_t* img, int w, int h, double u, double v, double* out) {
+  if (u < 0.0 || v < 0.0 || u > (double)(w - 1) || v > (double)(h - 1)) return false;
+  const int x0 = (int)floor(u), y0 = (int)floor(v);
+  const int x1 = min(x0 + 1, w - 1), y1 = min(y0 + 1, h - 1);
+  const double fx = __dsub_rn(u, (double)x0), fy = __dsub_rn(v, (double)y0);
+  const double p00 = img[y0 * w + x0], p10 = img[y0 * w + x1], p01 = img[y1 * w + x0], p11 = img[y1 * w + x1];
+  const double top = __dadd_rn(__dmul_rn(p00, __dsub_rn(1.0, fx)), __dmul_rn(p10, fx));
+  const double bot = __dadd_rn(__dmul_rn(p01, __dsub_rn(1.0, fx)), __dmul_rn(p11, fx));
+  *out = __dadd_rn(__dmul_rn(top, __dsub_rn(1.0, fy)), __dmul_rn(bot, fy));
+  return true;
+}
+
+__global__ void k_ncc_windows(const uint8_t* __restrict__ ref, int ref_w, int ref_h, const uint8_t* __restrict__ src,
+                              int src_w, int src_h, int patch_size, int n, const NccWindow* __restrict__ win,
+                              int* valid_out, double* ncc_out, int* weak_out, int* samples_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const NccWindow w = win[i];
+  const int half = patch_size / 2;
+  double sr = 0, ss = 0, srr = 0, sss = 0, srs = 0;
+  int valid = 0;
+  for (int dy = -half; dy <= half; ++dy)
+    for (int dx = -half; dx <= half; ++dx) {
+      double vr, vs;
+      if (!sample_bilinear_d(ref, ref_w, ref_h, __dadd_rn(w.ref_u, (double)dx), __dadd_rn(w.ref_v, (double)dy), &vr))
+        continue;
+      if (!sample_bilinear_d(src, src_w, src_h, __dadd_rn(w.src_u, (double)dx), __dadd_rn(w.src_v, (double)dy), &vs))
+        continue;
+      sr = __dadd_rn(sr, vr);
+      ss = __dadd_rn(ss, vs);
+      srr = __dadd_rn(srr, __dmul_rn(vr, vr));
+      sss = __dadd_rn(sss, __dmul_rn(vs, vs));
+      srs = __dadd_rn(srs, __dmul_rn(vr, vs));
+      ++valid;
+    }
+  int ok = 0, weak = 0;
+  double ncc = 0.0;
+  if (valid >= patch_size * patch_size / 2) {
+    const double nn = (double)valid;
+    const double mr = __ddiv_rn(sr, nn), ms = __ddiv_rn(ss, nn);
+    const double var_r = __dsub_rn(__ddiv_rn(srr, nn), __dmul_rn(mr, mr));
+    const double var_s = __dsub_rn(__ddiv_rn(sss, nn), __dmul_rn(ms, ms));
+    weak = var_r < 12.0;
+    const double denom = __dsqrt_rn(__dmul_rn(var_r, var_s));
+    if (!(denom < 1e-9)) {
+      ncc = __ddiv_rn(__dsub_rn(__ddiv_rn(srs, nn), __dmul_rn(mr, ms)), denom);
+      ncc = fmin(1.0, fmax(-1.0, ncc));
+      ok = 1;
+    }
+  }
+  valid_out[i] = ok;
+  ncc_out[i] = ok ? ncc : 0.0;
+  weak_out[i] = weak;
+  samples_out[i] = ok ? valid : 0;
+}
+
+__global__ void k_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out) {
+  *out = tex2Dgather<float4>(tex, x, y, 0);
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+static size_t pcache_bytes(int num_src, int threads) { return (size_t)num_src * 3 * threads * sizeof(float2); }
+
+cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const int* py, const double* inv,
+                             const float* normals, float* cost, int* support, float* view_cost, cudaStream_t st) {
+  const int threads = 128;
+  const int blocks = (n + threads - 1) / threads;
+  if (blocks == 0) return cudaSuccess;
+  k_eval_hyps<<<blocks, threads, pcache_bytes(J.num_src, threads), st>>>(J, mode, n, px, py, inv, normals, cost,
+                                                                          support, view_cost);
+  return cudaGetLastError();
+}
+
+static dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st) {
+  const dim3 b(32, 4);
+  k_plane_init<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(J, seed_depth, seed_grid, seed_gx);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters, cudaStream_t st) {
+  const dim3 b(32, 4);
+  const dim3 g((J.w + 63) / 64, (J.h + 3) / 4);
+  k_plane_sweep<<<g, b, pcache_bytes(J.num_src, 128), st>>>(J, color, iter, num_iters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st) {
+  const dim3 b(32, 4);
+  k_plane_refine<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(J, inv_per_px, iters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plane_output(const Job& J, float* depth, uint8_t* support, float* conf, float* normal,
+                                float* cost, unsigned int* filled, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_plane_output<<<grid2d(J.w, J.h, b), b, 0, st>>>(J, depth, support, conf, normal, cost, filled);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compat_init(const Job& J, float* cost, cudaStream_t st) {
+  const dim3 b(32, 4);
+  k_compat_init<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(J, cost);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compat_sweep(const Job& J, const double* inv_in, const float* cost_in, const int32_t* sup_in,
+                                double* inv_out, float* cost_out, int32_t* sup_out, const uint32_t* draws,
+                                const uint8_t* fire, int draw_stride, int search_count, double radius_ratio,
+                                int propagate, cudaStream_t st) {
+  const dim3 b(32, 4);
+  k_compat_sweep<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(
+      J, inv_in, cost_in, sup_in, inv_out, cost_out, sup_out, draws, fire, draw_stride, search_count, radius_ratio,
+      propagate);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compat_output(const Job& J, const double* inv, const float* cost, const int32_t* sup, float* depth,
+                                 uint8_t* support, float* conf, unsigned int* filled, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_compat_output<<<grid2d(J.w, J.h, b), b, 0, st>>>(J, inv, cost, sup, depth, support, conf, filled);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compat_refine(const Job& J, float* depth, float* conf, double inv_per_px, int fit_points,
+                                 int iters, unsigned int* refined, double* best_inv, float* best_cost,
+                                 cudaStream_t st) {
+  const dim3 b(32, 4);
+  k_compat_refine<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(
+      J, depth, conf, inv_per_px, fit_points, iters, refined, best_inv, best_cost);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_ref(const uint8_t* img, int w, int h, float* ref, float* box, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_prep_ref<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, ref, box);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+                            cudaStream_t st) {
+  const dim3 b(32, 8);
+  if (fp16)
+    k_prep_src_f16<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, (__half*)out, pitch_bytes / sizeof(__half));
+  else
+    k_prep_src_f32<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, (float*)out, pitch_bytes / sizeof(float));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_ref_f32(const float* img, int w, int h, float* ref, float* box, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_prep_ref_f32<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, ref, box);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+                                  cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_prep_src_f32in<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (fp16 ? 2 : 4), fp16);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,
+                               int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,
+                               int* samples, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_ncc_windows<<<(n + 127) / 128, 128, 0, st>>>(ref, ref_w, ref_h, src, src_w, src_h, patch_size, n, win, valid, ncc,
+                                                 weak, samples);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st) {
+  k_gather_probe<<<1, 1, 0, st>>>(tex, x, y, out);
+  return cudaGetLastError();
+}
+
+}  // namespace rmvs

@@ -1,0 +1,238 @@
+"""GPU parity: the CUDA engine through its C ABI against the reference's
+golden vectors and the CPU oracle.
+
+Tolerances (stated per test):
+  * integer/index/byte work and the FP64 paths -- bit-exact;
+  * FP32 window costs vs the reference's FP64 -- |dc| <= 1e-5 * |c| + 2e-6
+    for at least 99.9 % of hypotheses (the absolute floor covers costs near
+    0, where the relative bound is meaningless), and never above 1e-3;
+  * whole depth maps (order-dependent searches) -- statistics vs truth.
+"""
+import numpy as np
+import pytest
+
+import golden_io as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL, ABS = 1e-5, 2e-6
+
+
+@pytest.fixture(scope="module")
+def mvs():
+    import recon_mvs
+
+    recon_mvs.load_library()
+    return recon_mvs
+
+
+def gpu_views(mvs, d, prefix=""):
+    return mvs.ViewArgs(d[prefix + "ref"], list(d[prefix + "srcs"]), d[prefix + "ref_pose"], list(d[prefix + "poses"]),
+                        d[prefix + "ref_intr"], list(d[prefix + "intr"]), list(d[prefix + "source_indices"]))
+
+
+def gpu_config(mvs, d):
+    return mvs.MvsConfig(**G.config(d))
+
+
+def assert_costs_close(got, want, label):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    inf_w = want >= 1e29
+    inf_g = got >= 1e29
+    mism = (inf_w != inf_g).mean()
+    both = ~inf_w & ~inf_g
+    err = np.abs(got[both] - want[both])
+    ok = err <= REL * np.abs(want[both]) + ABS
+    print(f"{label}: n={both.sum()} inf-mismatch={mism:.4%} ok={ok.mean():.5%} "
+          f"max|d|={err.max() if err.size else 0:.3e} p99|d|={np.quantile(err, 0.99) if err.size else 0:.3e}")
+    assert mism <= 1e-3
+    assert ok.mean() >= 0.999
+    assert err.max() <= 1e-3
+
+
+@pytest.mark.parametrize("name", ["eval_plane.npz", "eval_distort.npz"])
+def test_compat_cost_matches_reference(mvs, name):
+    """EvaluateCandidate (patchmatch_stereo.cpp:344-418) on the reference's
+    own hypotheses: translated windows, distortion, both index forms."""
+    d = G.load(name)
+    cost, sup = mvs.Evaluate(gpu_views(mvs, d), gpu_config(mvs, d), mvs.Options(mode=mvs.MODE_COMPAT),
+                             d["px"], d["py"], d["inv"])
+    assert_costs_close(cost, d["cost"], name)
+    valid = d["cost"] < 1e29
+    assert (sup[valid] == d["valid_views"][valid]).mean() >= 0.999
+
+
+def test_compute_ncc_bit_exact(mvs):
+    d = G.load("ncc_known.npz")
+    imgs = [d["a"], d["brighter"], d["flat"]]
+    for i, ((ri, si), c) in enumerate(zip(d["which"], d["coords"])):
+        r = mvs.ComputeNcc(imgs[ri], imgs[si], *c, patch_size=11)
+        assert r.valid == d["valid"][i] and r.ncc == d["ncc"][i]
+        assert r.weak_texture == d["weak"][i] and r.valid_samples == d["samples"][i]
+
+
+def plane_hypotheses(sc, n, seed):
+    """Seeded plane hypotheses around the analytic truth plus random ones."""
+    rng = np.random.default_rng(seed)
+    h, w = sc.ref.depth.shape
+    px = rng.integers(0, w, n)
+    py = rng.integers(0, h, n)
+    td = sc.ref.depth[py, px]
+    tn = sc.ref.normal[py, px]
+    inv = np.where(np.isfinite(td), 1.0 / np.where(np.isfinite(td), td, 1.0), 0.0)
+    inv = inv * (1.0 + rng.normal(0, 0.01, n))
+    rand = rng.random(n) < 0.3
+    inv[rand] = rng.uniform(1 / sc.max_depth, 1 / sc.min_depth, rand.sum())
+    nrm = tn + rng.normal(0, 0.1, (n, 3))
+    nrm[~np.isfinite(nrm).all(1)] = [0.0, 0.0, -1.0]
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    bad = ~np.isfinite(td)
+    inv[bad] = rng.uniform(1 / sc.max_depth, 1 / sc.min_depth, bad.sum())
+    return px, py, inv, nrm
+
+
+def test_plane_cost_matches_fp64_oracle(mvs, orc):
+    """Plane-induced homography cost vs the FP64 oracle restatement on
+    identical hypotheses (FP16 and FP32 storage give identical 8-bit texels)."""
+    import synthetic as S
+
+    sc = S.sphere_on_backdrop(width=160, height=120, f=150.0, num_sources=4, seed=3)
+    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    px, py, inv, nrm = plane_hypotheses(sc, 4000, 7)
+    cfg_d = dict(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, patch_size=11)
+    vs_o = O.ViewSet(imgs[0], imgs[1:], cams[0], cams[1:])
+    for best_k in (0, 2):
+        want, want_sup, want_view = orc.plane_costs(vs_o, O.make_config(**cfg_d), best_k, px, py, inv, nrm)
+        for storage in (mvs.STORAGE_FP32, mvs.STORAGE_FP16):
+            opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=best_k, storage=storage)
+            va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+            got, sup, view = mvs.Evaluate(va, mvs.MvsConfig(**cfg_d), opts, px, py, inv, nrm.astype(np.float32),
+                                          per_view=True)
+            assert_costs_close(got, want, f"plane best_k={best_k} storage={storage}")
+            assert_costs_close(view.ravel(), want_view.ravel(), "per-view")
+
+
+def test_compat_patchmatch_on_reference_scene(mvs):
+    """COMPAT PatchMatchStereo on the reference unit test's plane scene: the
+    reference's own golden map (2 iterations x 4 directions, 4 row blocks)
+    and the GPU map agree pixel for pixel except where FP32 and FP64 costs
+    order near-tied candidates differently, and pass the unit test's
+    accuracy gates (test_mvs.cpp:337-466)."""
+    d = G.load("pm_plane.npz")
+    vs = gpu_views(mvs, d)
+    cfg = gpu_config(mvs, d)
+    dm = mvs.PatchMatchStereo(vs, cfg, options=mvs.Options(mode=mvs.MODE_COMPAT))
+    ref = d["depth"]
+    both = np.isfinite(ref) & np.isfinite(dm.depth)
+    same = np.abs(dm.depth[both] - ref[both]) <= 1e-6 * ref[both]
+    print("filled", dm.filled, int(d["filled"]), "identical", same.mean())
+    assert abs(dm.filled - int(d["filled"])) <= 0.01 * d["filled"]
+    assert same.mean() >= 0.95
+    n = mvs.RefineSubpixel(vs, cfg, dm, options=mvs.Options(mode=mvs.MODE_COMPAT))
+    truth = d["truth"]
+    err = (np.abs(dm.depth - truth) * 1000.0)[20:-20, 20:-20]
+    err = np.sort(err[np.isfinite(err)])
+    med, p95 = err[len(err) // 2], err[int(len(err) * 0.95)]
+    print("refined", n, "median mm", med, "p95 mm", p95)
+    assert med <= 19.1 * 0.15 * 1.5 and p95 <= 19.1 * 0.15 * 3.0
+
+
+def test_compat_refine_matches_reference(mvs, orc):
+    """RefineSubpixel on the reference's own PatchMatch output: each pixel
+    is independent, so the refined inverse depth must match the reference
+    per pixel to within the final golden-section bracket."""
+    d = G.load("pm_plane.npz")
+    vs = gpu_views(mvs, d)
+    cfg = gpu_config(mvs, d)
+    dm = mvs.DepthMap(d["depth"].copy(), d["support"].copy(), d["conf"].copy())
+    n = mvs.RefineSubpixel(vs, cfg, dm, options=mvs.Options(mode=mvs.MODE_COMPAT))
+    assert abs(n - int(d["refined"])) <= 0.001 * d["refined"]
+    ref = d["rdepth"]
+    both = np.isfinite(ref) & np.isfinite(dm.depth)
+    rel = np.abs(dm.depth[both] - ref[both]) / ref[both]
+    print("refine: identical", (rel <= 1e-6).mean(), "within 0.5%", (rel <= 5e-3).mean())
+    assert (rel <= 1e-6).mean() >= 0.97
+    assert (rel <= 5e-3).mean() >= 0.999
+
+
+def test_fuse_bit_exact(mvs):
+    """FuseDepthMaps on the reference's refined maps: the fused cloud is
+    bit-identical to the reference's (compared sorted by position)."""
+    for name in ("pm_plane.npz", "pm_sphere.npz"):
+        d = G.load(name)
+        cfg = gpu_config(mvs, d)
+        maps = [mvs.DepthMap(d["rdepth"], d["support"], d["rconf"])]
+        poses, intr = [d["ref_pose"]], [d["ref_intr"]]
+        if "b_depth" in d:
+            maps.append(mvs.DepthMap(d["b_depth"], d["b_support"], d["b_conf"]))
+            poses.append(d["b_ref_pose"])
+            intr.append(d["b_ref_intr"])
+        pc = mvs.FuseDepthMaps(maps, poses, intr, cfg)
+        order = np.lexsort((pc.positions[:, 2], pc.positions[:, 1], pc.positions[:, 0]))
+        pos, nrm, conf = pc.positions[order], pc.normals[order], pc.confidences[order]
+        assert len(pos) == int(d["fcount"])
+        assert G.digest(pos, nrm, conf) == str(d["fdigest"]), name
+        assert pc.counts.sum() > 0
+
+
+def consistency_maps(sc_views):
+    """Truth-derived depth maps with holes and outliers, for consistency tests."""
+    rng = np.random.default_rng(5)
+    maps = []
+    for v in sc_views:
+        dd = v.depth.astype(np.float32).copy()
+        dd[rng.random(dd.shape) < 0.05] = np.nan
+        bad = rng.random(dd.shape) < 0.05
+        dd[bad] *= rng.uniform(0.9, 1.1, bad.sum()).astype(np.float32)
+        maps.append(dd)
+    return maps
+
+
+def test_geometric_consistency_bit_exact(mvs):
+    import synthetic as S
+
+    sc = S.sphere_on_backdrop(width=120, height=90, f=110.0, num_sources=4, seed=8)
+    views = [sc.ref] + sc.sources
+    depths = consistency_maps(views)
+    poses = [v.camera.pose_array() for v in views]
+    intr = [v.camera.intrinsics_array() for v in views]
+    oracle_maps = [(dd, np.ones(dd.shape, np.uint8), np.ones(dd.shape, np.float32)) for dd in depths]
+    gpu_maps = [mvs.DepthMap(dd, np.ones(dd.shape, np.uint8), np.ones(dd.shape, np.float32)) for dd in depths]
+    for r in range(len(views)):
+        want_c, want_k = O.geo_consistency(oracle_maps, poses, intr, r, 0.01, 1.0, 3)
+        got_c, got_k = mvs.GeometricConsistency(gpu_maps, poses, intr, r, 0.01, 1.0, 3)
+        assert np.array_equal(got_c, want_c) and np.array_equal(got_k, want_k)
+        assert want_k.mean() > 0.3
+
+
+def test_undistort_bit_exact(mvs, orc):
+    import synthetic as S
+
+    sc = S.tabletop(width=192, height=144, f=145.0, num_sources=1, seed=4)
+    k = sc.ref.camera.intrinsics_array()
+    want = orc.undistort(sc.ref.image, k)
+    got = mvs.Undistort(sc.ref.image, k)
+    assert np.array_equal(got, want)
+    assert np.abs(got - sc.ref.image).mean() > 0.1  # the remap moved pixels
+
+
+def test_contract_violations(mvs):
+    d = G.load("eval_plane.npz")
+    cfg = gpu_config(mvs, d)
+    bad = mvs.ViewArgs(d["ref"], list(d["srcs"]), d["ref_pose"], list(d["poses"]), d["ref_intr"], list(d["intr"]),
+                       [1, 2, 3, 9])
+    with pytest.raises(mvs.MvsError) as e:
+        mvs.PatchMatchStereo(bad, cfg)
+    assert e.value.status == mvs.RECON_ERR_INVALID_ARGUMENT
+    bad2 = mvs.ViewArgs(d["ref"], list(d["srcs"]), d["ref_pose"], list(d["poses"]), d["ref_intr"],
+                        list(d["intr"])[:3], [1, 2, 3, 4])
+    with pytest.raises(mvs.MvsError):
+        mvs.PatchMatchStereo(bad2, cfg)
+    # empty depth range: RECON_OK, nothing filled (patchmatch_stereo.cpp:485)
+    cfg2 = gpu_config(mvs, d)
+    cfg2.min_depth_m, cfg2.max_depth_m = 0.9, 0.5
+    dm = mvs.PatchMatchStereo(gpu_views(mvs, d), cfg2)
+    assert dm.filled == 0 and np.isnan(dm.depth).all()
