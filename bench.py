@@ -104,7 +104,22 @@ class ClockSampler:
 def make_scene(device):
     import synthetic as Syn
 
+    if WORKLOAD == "small":
+        return Syn.sphere_on_backdrop(width=W, height=H, f=F, num_sources=S_SRC, seed=1, device=device)
     return Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device)
+
+
+WORKLOAD = "c2"
+
+
+def set_workload(name):
+    """c2: the headline 1920x1440 x 8 sources; small: the 640x480 x 4
+    sources sphere scene (profiling captures, CPU-runnable size)."""
+    global WORKLOAD, W, H, F, ITERS, S_SRC, FLOP_PER_HYP
+    WORKLOAD = name
+    if name == "small":
+        W, H, F, ITERS, S_SRC = 640, 480, 600.0, 6, 4
+    FLOP_PER_HYP = S_SRC * (K * K * 26 + 30) + 40
 
 
 def views_of(M, sc):
@@ -304,7 +319,7 @@ def run_gpu(args):
         t1 = time.perf_counter()
         if i > 0:
             e2e_times.append(t1 - t0)
-    e2e_s = barrier_max(world, statistics.mean(e2e_times))
+    e2e_s = barrier_max(world, statistics.mean(e2e_times)) if e2e_times else float("nan")
     e2e_value = world / e2e_s
     h2d = (1 + S_SRC) * W * H
     d2h = W * H * (4 + 1 + 4 + 12 + 4) + 4
@@ -335,7 +350,8 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp16-storage/f32" if args.fp16 else "f32",
             "data": "synthetic (seeded tabletop scene, analytic truth)",
-            "config": {"workload": f"tabletop {W}x{H}, {S_SRC} sources, {K}x{K}, {ITERS} iterations, "
+            "config": {"workload": f"{'tabletop' if WORKLOAD == 'c2' else 'sphere'} {W}x{H}, {S_SRC} sources, "
+                                   f"{K}x{K}, {ITERS} iterations, "
                                    f"plane mode, best_k={args.best_k}, golden-section refine",
                        "storage": "fp16" if args.fp16 else "fp32",
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
@@ -371,7 +387,9 @@ def main():
     ap.add_argument("--fp16", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "small"])
     args = ap.parse_args()
+    set_workload(args.workload)
     if args.impl == "reference":
         run_reference_arm(args)
     else:

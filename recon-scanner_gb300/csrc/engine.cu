@@ -1212,17 +1212,19 @@ RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const rec
       for (int i = 0; i < 3; ++i) M.t[i] = poses[m].t[i];
       CK(launch_fuse_points(M, base[m], P, key.p, pos.p, nrm.p, conf.p, valid.p, C.stream));
     }
+    CK(cudaMemsetAsync(slot_of.p, 0xFF, total * sizeof(int), C.stream));  // -1: no slot
     CK(launch_fuse_insert(total, key.p, valid.p, tkey.p, tcount.p, tfirst.p, cap - 1, slot_of.p, err.p, C.stream));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    if (herr) fail(RECON_ERR_INTERNAL, "voxel hash table overflow");
     CK(launch_fuse_flags(total, valid.p, slot_of.p, tfirst.p, flag.p, C.stream));
     scratch.alloc(scan_scratch_elems(total));
     CK(exclusive_scan_u32(flag.p, vid_of.p, total, scratch.p, C.stream));
     unsigned int last_vid = 0, last_flag = 0;
-    int herr = 0;
     CK(cudaMemcpyAsync(&last_vid, vid_of.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
     CK(cudaMemcpyAsync(&last_flag, flag.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, C.stream));
     CK(cudaStreamSynchronize(C.stream));
-    if (herr) fail(RECON_ERR_INTERNAL, "voxel hash table overflow");
     const unsigned int nvox = last_vid + last_flag;
     if (nvox == 0) return;
     DevArray<unsigned int> vcount, voffset, cursor;

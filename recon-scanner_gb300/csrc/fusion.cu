@@ -16,7 +16,9 @@
 
 namespace rmvs {
 
-constexpr unsigned long long kEmptyKey = 0x7FFFFFFFFFFFFFFFull;
+// Empty-slot key: the table is cleared with a byte memset of 0x7F, so the
+// sentinel must be that byte pattern.
+constexpr unsigned long long kEmptyKey = 0x7F7F7F7F7F7F7F7Full;
 
 // ---------------------------------------------------------------------------
 // FP64 helpers in the reference's evaluation order (linalg.h:224-232)
@@ -108,6 +110,7 @@ __global__ void k_fuse_insert(int64_t n, const unsigned long long* __restrict__ 
     }
     s = (s + 1) & mask;
   }
+  slot_of[g] = -1;
   atomicExch(error, 1);
 }
 
@@ -116,7 +119,8 @@ __global__ void k_fuse_flags(int64_t n, const uint8_t* __restrict__ valid, const
                              const unsigned long long* __restrict__ table_first, unsigned int* flag) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
-  flag[g] = (valid[g] && table_first[slot_of[g]] == (unsigned long long)g) ? 1u : 0u;
+  const int s = slot_of[g];
+  flag[g] = (valid[g] && s >= 0 && table_first[s] == (unsigned long long)g) ? 1u : 0u;
 }
 
 __global__ void k_fuse_voxels(int64_t n, const unsigned int* __restrict__ flag, const unsigned int* __restrict__ vid_of,
@@ -134,7 +138,7 @@ __global__ void k_fuse_scatter(int64_t n, const uint8_t* __restrict__ valid, con
                                const unsigned int* __restrict__ slot_vid, const unsigned int* __restrict__ voffset,
                                unsigned int* cursor, int64_t* bucket) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n || !valid[g]) return;
+  if (g >= n || !valid[g] || slot_of[g] < 0) return;
   const unsigned int v = slot_vid[slot_of[g]];
   const unsigned int p = atomicAdd(&cursor[v], 1u);
   bucket[voffset[v] + p] = g;

