@@ -338,11 +338,17 @@ __global__ void __launch_bounds__(128) k_plane_sweep(Job J, int color, int iter,
   Rng g = pixel_rng(J, idx, iter, 2 + color);
   const float scale = exp2f(-(float)iter);  // 1, 1/2, 1/4, ...
   const float span = J.rho_max - J.rho_min;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 5; ++k) {
     float rho = cur.x, nx = cur.y, ny = cur.z, nz = cur.w;
     if (k == 0) {
       rho = J.rho_min + span * g.uniform();
       random_normal(g, rx, ry, &nx, &ny, &nz);
+    } else if (k == 4) {
+      // the current depth on a fronto-parallel plane (the reference's model)
+      if (nx == 0.f && ny == 0.f) continue;
+      nx = 0.f;
+      ny = 0.f;
+      nz = -1.f;
     } else {
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
