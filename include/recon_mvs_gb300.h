@@ -305,6 +305,33 @@ RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_
 RECON_API recon_status recon_mvs_job_release(void* ctx, int32_t job);
 RECON_API recon_status recon_mvs_synchronize(void* ctx);
 RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out);
+/* Geometric consistency for callers that cannot let a library allocate
+ * device memory -- for example a capture or streaming loop that keeps every
+ * buffer in its own pre-sized pool (a cudaMalloc would synchronise the
+ * device and stall it), or a process whose GPU memory is rationed by its own
+ * allocator.  No counterpart in the reference.
+ *
+ * Same test as recon_mvs_geometric_consistency, but every map's `depth`
+ * and out_count / out_keep (width*height of the reference map) are DEVICE
+ * pointers owned by the caller; poses and intrinsics are host memory.  The
+ * work is queued on `stream` (a cudaStream_t; NULL = the default stream) and
+ * the call returns without waiting for it.  Nothing is allocated: the
+ * per-source descriptor table lives in a fixed array in the library's
+ * device image, sized for at most 64 source maps (num_maps - 1 <= 64; more
+ * is RECON_ERR_INVALID_ARGUMENT).  Every GPU that loads the library keeps
+ * that array until the process exits.
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's
+ * contents; calls whose GPU work overlaps race on it, so serialise them. */
+RECON_API recon_status recon_mvs_geometric_consistency_noalloc(const recon_mvs_depth_map* maps,
+                                                               const recon_pose* poses,
+                                                               const recon_camera_intrinsics* intr, int32_t num_maps,
+                                                               int32_t ref_index, float rel_depth_max,
+                                                               float reproj_px_max, int32_t min_views,
+                                                               uint8_t* out_count, uint8_t* out_keep, void* stream);
+
 /* Human-readable description of the last error on this thread. */
 RECON_API const char* recon_mvs_last_error(void);
 

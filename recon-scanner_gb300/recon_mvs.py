@@ -154,6 +154,10 @@ _SIGS = {
     "recon_mvs_geometric_consistency": (C.c_int, [C.POINTER(DepthMapC), C.POINTER(Pose), C.POINTER(Intrinsics),
                                                   C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32,
                                                   C.POINTER(C.c_uint8), C.POINTER(C.c_uint8)]),
+    "recon_mvs_geometric_consistency_noalloc": (C.c_int, [C.POINTER(DepthMapC), C.POINTER(Pose),
+                                                          C.POINTER(Intrinsics), C.c_int32, C.c_int32, C.c_float,
+                                                          C.c_float, C.c_int32, C.c_void_p, C.c_void_p,
+                                                          C.c_void_p]),
     "recon_mvs_fuse": (C.c_int, [C.POINTER(DepthMapC), C.POINTER(Pose), C.POINTER(Intrinsics), C.c_int32,
                                  C.POINTER(MvsConfig), C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(PointCloudC)]),
     "recon_mvs_point_cloud_free": (None, [C.POINTER(PointCloudC)]),
