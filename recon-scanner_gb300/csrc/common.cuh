@@ -77,12 +77,21 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
 // a + b * c with b ff, c float
 __device__ __forceinline__ ff ff_fma_f(ff a, ff b, float c) { return ff_add(a, ff_mul_f(b, c)); }
 
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// a / b: an approximate quotient, then the exactly computed remainder
+// corrects it (the final error is second order in the approximation).
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const float rb = rcp_approx(b.hi);
+  const float q1 = a.hi * rb;
   // r = a - q1 * b
   const ff qb = ff_mul_f(b, q1);
   const ff r = ff_add(a, ff{-qb.hi, -qb.lo});
-  const float q2 = __fdiv_rn(r.hi, b.hi);
+  const float q2 = r.hi * rb;
   return fast_two_sum(q1, q2);
 }
 
@@ -152,6 +161,8 @@ struct Job {
   double rk1, rk2, rk3, rp1, rp2;
   const float* ref;      // (I - 128), row-major w x h
   const float* ref_box;  // compat: 2x2 box average of (I - 128), (w-1) x (h-1) used
+  const float* ref_de;   // plane mode: even / odd column planes of ref, [2][h][ref_half_w]
+  int ref_half_w;
   const SrcView* src;    // num_src entries (device memory)
   // plane-mode state
   float4* hyp;   // {rho, nx, ny, nz}

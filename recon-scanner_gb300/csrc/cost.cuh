@@ -253,8 +253,111 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
   *cnt = n;
 }
 
+// Reference-window accessors for the unrolled window: value of sample
+// k = dx + H of a row, split into even k (even(m), k = 2m) and odd k
+// (odd(m), k = 2m + 1) so that, with H known at compile time, every offset
+// is a constant.
+struct GlobalRow {
+  const float* p;  // row start at x - H
+  __device__ __forceinline__ float even(int m) const { return __ldg(p + 2 * m); }
+  __device__ __forceinline__ float odd(int m) const { return __ldg(p + 2 * m + 1); }
+};
+
+struct GlobalRef {
+  const float* ref;
+  int w, x, y;
+  template <int H>
+  __device__ __forceinline__ GlobalRow row(int dy) const {
+    return GlobalRow{ref + (size_t)(y + dy) * w + (x - H)};
+  }
+};
+
+// Shared-memory tile of the reference image stored as even / odd column
+// planes, so that the 32 lanes of a warp (32 same-colour pixels of one row,
+// two columns apart) read consecutive words: conflict-free.
+constexpr int kTileCols = 48;  // plane columns: the warp's 32 + 8 margin each side
+struct TileRow {
+  const float* a;
+  const float* b;
+  __device__ __forceinline__ float even(int m) const { return a[m]; }
+  __device__ __forceinline__ float odd(int m) const { return b[m]; }
+};
+
+struct TileRef {
+  const float* same;   // the column plane of this thread's own parity, [rows][kTileCols]
+  const float* other;  // the other plane
+  int lane, parity, ty;
+  template <int H>
+  __device__ __forceinline__ TileRow row(int dy) const {
+    const int r = (ty + H + dy) * kTileCols + lane + 8;
+    if (H & 1) return TileRow{other + r + parity - (H + 1) / 2, same + r - (H - 1) / 2};
+    return TileRow{same + r - H / 2, other + r + parity - H / 2};
+  }
+};
+
+// One window row of the fast path, fully unrolled.  Floors by magic-number
+// rounding (FMA pipe): m = t' + 1.5*2^23 rounds t' = t - 0.5 to the nearest
+// integer, i.e. floor(t); at exact ties the footprint shifts by one texel
+// with weight 1, which reads the same value (bilinear is continuous).
+template <int H, class Row>
+__device__ __forceinline__ void plane_row(cudaTextureObject_t tex, const Row& row, float& den, float& nu, float& nv,
+                                          float c0, float A0, float B0, float fum, float fvm, float gxo, float gyo,
+                                          float rmean, float sc, float& r_s, float& r_ss, float& r_rs) {
+  constexpr float kM = 12582912.0f;
+#pragma unroll
+  for (int k = 0; k <= 2 * H; ++k) {
+    const float rinv = rcp_approx(den);
+    const float tmu = fmaf(nu, rinv, fum);
+    const float tmv = fmaf(nv, rinv, fvm);
+    const float mu = __fadd_rn(tmu, kM), mv = __fadd_rn(tmv, kM);
+    const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
+    const float wu = __fadd_rn(__fsub_rn(tmu, flu), 0.5f);
+    const float wv = __fadd_rn(__fsub_rn(tmv, flv), 0.5f);
+    const float4 g = tex2Dgather<float4>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo), 0);
+    const float top = fmaf(wu, g.z - g.w, g.w);
+    const float bot = fmaf(wu, g.y - g.x, g.x);
+    const float sv = fmaf(wv, bot - top, top) - sc;
+    const float rv = ((k & 1) ? row.odd(k >> 1) : row.even(k >> 1)) - rmean;
+    r_s += sv;
+    r_ss = fmaf(sv, sv, r_ss);
+    r_rs = fmaf(rv, sv, r_rs);
+    den += c0;
+    nu += A0;
+    nv += B0;
+  }
+}
+
+template <int H, class Ref>
+__device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, const Ref& ref, int iu, int iv, float fu,
+                                                  float fv, float A0, float A1, float B0, float B1, float c0, float c1,
+                                                  float rmean, float sc, float* acc) {
+  constexpr float kM = 12582912.0f;
+  const float fum = fu - 0.5f, fvm = fv - 0.5f;
+  const float gxo = ((float)iu + 1.0f) - kM, gyo = ((float)iv + 1.0f) - kM;
+  float ss = 0.f, sss = 0.f, srs = 0.f;
+#pragma unroll 1
+  for (int dy = -H; dy <= H; ++dy) {
+    const float fdy = (float)dy;
+    float den = fmaf(fdy, c1, fmaf(-(float)H, c0, 1.0f));
+    float nu = fmaf(fdy, A1, -(float)H * A0);
+    float nv = fmaf(fdy, B1, -(float)H * B0);
+    float r_s = 0.f, r_ss = 0.f, r_rs = 0.f;
+    plane_row<H>(tex, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, rmean, sc, r_s, r_ss,
+                 r_rs);
+    ss += r_s;
+    sss += r_ss;
+    srs += r_rs;
+  }
+  acc[2] = ss;
+  acc[3] = sss;
+  acc[4] = srs;
+}
+
+// H > 0: windows of 2H+1 known at compile time, reference samples through
+// `ref` on the fast path; H == 0: any window size (runtime loop).
+template <int H, class Ref>
 __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
-                                                      const PlaneHyp& hp, const RefWindow& rw) {
+                                                      const PlaneHyp& hp, const RefWindow& rw, const Ref& ref) {
   ViewResult bad{0.0f, 0};
   ff u0, v0;
   float xz, mx, my;
@@ -266,7 +369,7 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const float G1x = fmaf(hp.s1, S.b[0], S.Ac1[0]);
   const float G1y = fmaf(hp.s1, S.b[1], S.Ac1[1]);
   const float G1z = fmaf(hp.s1, S.b[2], S.Ac1[2]);
-  const float iz = 1.0f / xz;
+  const float iz = rcp_approx(xz);
   const float A0 = S.fx * (G0x - mx * G0z) * iz;
   const float A1 = S.fx * (G1x - mx * G1z) * iz;
   const float B0 = S.fy * (G0y - my * G0z) * iz;
@@ -278,7 +381,7 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   float fu, fv;
   ff_floor_frac(ff_add(u0, ff_make(-0.5f)), &iu, &fu);
   ff_floor_frac(ff_add(v0, ff_make(-0.5f)), &iv, &fv);
-  const int h = J.patch_half;
+  const int h = H > 0 ? H : J.patch_half;
   const float fh = (float)h;
   // fast path: the four corners (hence, by convexity, the whole window)
   // inside the source, in front of it, and on the camera side of the plane
@@ -288,11 +391,12 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
     for (int c = 0; c < 4; ++c) {
       const float dx = (c & 1) ? fh : -fh, dy = (c & 2) ? fh : -fh;
       const float den = fmaf(dx, c0, fmaf(dy, c1, 1.0f));
-      const float tu = fu + fmaf(dx, A0, dy * A1) / den;
-      const float tv = fv + fmaf(dx, B0, dy * B1) / den;
+      const float rd = rcp_approx(den);
+      const float tu = fu + fmaf(dx, A0, dy * A1) * rd;
+      const float tv = fv + fmaf(dx, B0, dy * B1) * rd;
       const float nr = hp.kappa + dx * hp.ex + dy * hp.ey;
-      full = full && den > 0.0f && nr < 0.0f && tu >= (float)(-iu) && tu <= (float)(S.w - 1 - iu) &&
-             tv >= (float)(-iv) && tv <= (float)(S.h - 1 - iv);
+      full = full && den > 0.0f && nr < 0.0f && tu >= (float)(-iu) + 0.001f && tu <= (float)(S.w - 1 - iu) - 0.001f &&
+             tv >= (float)(-iv) + 0.001f && tv <= (float)(S.h - 1 - iv) - 0.001f;
     }
   }
   // source centring value: the sample at the window centre (clamped read)
@@ -301,7 +405,10 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const int K = 2 * h + 1;
   const int min_valid = J.min_valid;
   if (full) {
-    plane_window<true>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+    if constexpr (H > 0)
+      plane_window_fast<H>(S.tex, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
+    else
+      plane_window<true>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
   plane_window<false>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);

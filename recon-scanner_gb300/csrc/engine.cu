@@ -186,7 +186,7 @@ struct JobData {
   bool degenerate = false;  // zero baseline or empty depth range: output all-invalid
   double inv_per_px = 0.0;
   DevArray<uint8_t> ref_u8;
-  DevArray<float> ref, ref_box;
+  DevArray<float> ref, ref_box, ref_de;
   std::vector<std::unique_ptr<Texture>> tex;
   std::vector<SrcView> host_src;
   DevArray<SrcView> src_table;
@@ -363,6 +363,11 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   else
     CK(launch_prep_ref((const uint8_t*)ref_dev, D.w, D.h, D.ref.p, compat ? D.ref_box.p : nullptr, C.stream));
   if (undistort) rk.k1 = rk.k2 = rk.k3 = rk.p1 = rk.p2 = 0.0;
+  const int half_w = (D.w + 1) / 2;
+  if (plane) {
+    D.ref_de.alloc((size_t)2 * half_w * D.h);
+    CK(launch_deinterleave(D.ref.p, D.w, D.h, half_w, D.ref_de.p, C.stream));
+  }
 
   // ---- sources ----
   D.host_src.resize(v->num_src);
@@ -442,6 +447,8 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   J.rp2 = rk.p2;
   J.ref = D.ref.p;
   J.ref_box = D.ref_box.p;
+  J.ref_de = D.ref_de.p;
+  J.ref_half_w = half_w;
   J.src = D.src_table.p;
   J.dinv_min = inv_min;
   J.dinv_max = inv_max;

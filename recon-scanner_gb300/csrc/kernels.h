@@ -72,6 +72,7 @@ cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t 
                             cudaStream_t st);
 cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
                                   cudaStream_t st);
+cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, float* out, cudaStream_t st);
 cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);
 cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,
                                int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,

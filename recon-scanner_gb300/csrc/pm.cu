@@ -15,6 +15,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdio>
+#include <type_traits>
 
 #include "cost.cuh"
 #include "kernels.h"
@@ -82,8 +83,9 @@ __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int 
   return r;
 }
 
+template <int H, class Ref>
 __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
-                                  float nx, float ny, float nz, const RefWindow& rw, float* view_cost,
+                                  float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
                                   int* nevals = nullptr) {
   HypCost bad{kCostInf, 0};
   if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max) return bad;
@@ -98,7 +100,7 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
   for (int s = 0; s < J.num_src; ++s) {
     ff P[3];
     pc.get(s, P);
-    const ViewResult v = eval_view_plane(J, J.src[s], x, y, P, hp, rw);
+    const ViewResult v = eval_view_plane<H>(J, J.src[s], x, y, P, hp, rw, ref);
     float c = kCostInf;
     if (v.valid) {
       c = 1.0f - v.ncc;
@@ -149,6 +151,7 @@ __device__ HypCost eval_compat_hyp(const Job& J, const PCache& pc, int x, int y,
 // ---------------------------------------------------------------------------
 // batch evaluation of given hypotheses (parity instrument, adjoint driver)
 // ---------------------------------------------------------------------------
+template <int H>
 __global__ void k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
                             const double* __restrict__ inv, const float* __restrict__ normals, float* out_cost,
                             int* out_support, float* out_view_cost) {
@@ -166,8 +169,9 @@ __global__ void k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, 
     r = eval_compat_hyp(J, pc, x, y, inv[i], rw, vc);
   } else {
     const RefWindow rw = ref_window(J, x, y, false);
-    r = eval_plane_hyp(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
-                       rw, vc);
+    const GlobalRef ref{J.ref, J.w, x, y};
+    r = eval_plane_hyp<H>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
+                          rw, ref, vc);
   }
   out_cost[i] = r.cost;
   out_support[i] = r.support;
@@ -225,6 +229,7 @@ __device__ __forceinline__ Rng pixel_rng(const Job& J, int idx, int iter, int sa
   return g;
 }
 
+template <int H>
 __global__ void k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -251,7 +256,8 @@ __global__ void k_plane_init(Job J, const float* __restrict__ seed_depth, int se
     }
   }
   const RefWindow rw = ref_window(J, x, y, false);
-  const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, nullptr);
+  const GlobalRef ref{J.ref, J.w, x, y};
+  const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
   J.hyp[idx] = make_float4(rho, nx, ny, nz);
   J.cost[idx] = c.cost;
   J.support[idx] = (uint8_t)min(c.support, 255);
@@ -273,17 +279,81 @@ __device__ __forceinline__ void plane_candidate_transfer(const float4 hn, float 
   *rho = (kn < 0.f && kp < 0.f) ? hn.x * kp / kn : -1.0f;
 }
 
-__global__ void __launch_bounds__(128) k_plane_sweep(Job J, int color, int iter, int num_iters) {
+// Reference-window statistics from the shared tile (same values as
+// ref_window for pixels whose window lies inside the image).
+template <int H>
+__device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t, int x, int y) {
+  RefWindow rw;
+  rw.full = x >= H && y >= H && x + H <= J.w - 1 && y + H <= J.h - 1;
+  if (!rw.full) return ref_window(J, x, y, false);
+  float s = 0.f;
+#pragma unroll 1
+  for (int dy = -H; dy <= H; ++dy) {
+    const TileRow r = t.row<H>(dy);
+#pragma unroll
+    for (int k = 0; k <= 2 * H; ++k) s += (k & 1) ? r.odd(k >> 1) : r.even(k >> 1);
+  }
+  rw.mean = s / (float)((2 * H + 1) * (2 * H + 1));
+  float q = 0.f;
+#pragma unroll 1
+  for (int dy = -H; dy <= H; ++dy) {
+    const TileRow r = t.row<H>(dy);
+    float qr = 0.f;
+#pragma unroll
+    for (int k = 0; k <= 2 * H; ++k) {
+      const float d = ((k & 1) ? r.odd(k >> 1) : r.even(k >> 1)) - rw.mean;
+      qr = fmaf(d, d, qr);
+    }
+    q += qr;
+  }
+  rw.sxx = q;
+  return rw;
+}
+
+// One red-black half-sweep.  A block of 32 x 4 threads owns the 32
+// same-colour pixels of each of 4 rows (64 columns); the reference rows it
+// reads (4 + 2H rows, the 64 columns +- 16) are staged once into shared
+// memory as even / odd column planes from the de-interleaved reference copy.
+template <int H>
+__global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int iter, int num_iters) {
   extern __shared__ float2 smem[];
+  constexpr int kRows = 4 + 2 * (H > 0 ? H : 1);
+  __shared__ float tile[2][kRows][kTileCols];
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int x = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + ((y + color) & 1);
+  const int parity = (y + color) & 1;
+  const int x = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + parity;
+  if constexpr (H > 0) {
+    const int i0 = blockIdx.x * 32 - 8;
+    const int r0 = blockIdx.y * 4 - H;
+    for (int e = tid; e < 2 * kRows * kTileCols; e += 128) {
+      const int p = e / (kRows * kTileCols);
+      const int rr = (e / kTileCols) % kRows;
+      const int j = e % kTileCols;
+      const int row = r0 + rr, col = i0 + j;
+      float v = 0.f;
+      if (row >= 0 && row < J.h && col >= 0 && col < J.ref_half_w) v = J.ref_de[((size_t)p * J.h + row) * J.ref_half_w + col];
+      tile[p][rr][j] = v;
+    }
+    __syncthreads();
+  }
   if (x >= J.w || y >= J.h) return;
   const int idx = y * J.w + x;
   float rx, ry;
   fill_pcache(J, pc, x, y, &rx, &ry);
-  const RefWindow rw = ref_window(J, x, y, false);
+  using RefT = std::conditional_t<(H > 0), TileRef, GlobalRef>;
+  RefT ref;
+  if constexpr (H > 0)
+    ref = TileRef{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
+                  (int)threadIdx.x, parity, (int)threadIdx.y};
+  else
+    ref = GlobalRef{J.ref, J.w, x, y};
+  RefWindow rw;
+  if constexpr (H > 0)
+    rw = tile_window<H>(J, ref, x, y);
+  else
+    rw = ref_window(J, x, y, false);
   float4 cur = J.hyp[idx];
   float cur_cost = J.cost[idx];
   int cur_sup = J.support[idx];
@@ -326,7 +396,7 @@ __global__ void __launch_bounds__(128) k_plane_sweep(Job J, int color, int iter,
     plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
     if (!(rho > 0.f)) continue;
     if (rho == cur.x && hn.y == cur.y && hn.z == cur.z && hn.w == cur.w) continue;
-    const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);
@@ -353,7 +423,7 @@ __global__ void __launch_bounds__(128) k_plane_sweep(Job J, int color, int iter,
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
     }
-    const HypCost c = eval_plane_hyp(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, nx, ny, nz);
@@ -668,6 +738,7 @@ __global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per
 // Plane-mode refinement: golden-section search on the inverse depth along
 // the pixel's own plane normal over +-1 px of disparity, the reference's
 // refinement schedule applied to the plane cost.
+template <int H>
 __global__ void k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -682,7 +753,10 @@ __global__ void k_plane_refine(Job J, double inv_per_px, int subpixel_iterations
   float rx, ry;
   fill_pcache(J, pc, x, y, &rx, &ry);
   const RefWindow rw = ref_window(J, x, y, false);
-  auto eval = [&](float v) -> HypCost { return eval_plane_hyp(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, nullptr); };
+  const GlobalRef ref{J.ref, J.w, x, y};
+  auto eval = [&](float v) -> HypCost {
+    return eval_plane_hyp<H>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
+  };
   float best_d = h0.x, best_c = c0;
   int best_s = J.support[idx];
   float lo = fmaxf(J.rho_min, best_d - (float)inv_per_px);
@@ -744,6 +818,18 @@ __global__ void k_prep_ref(const uint8_t* __restrict__ img, int w, int h, float*
     const int x1 = min(x + 1, w - 1), y1 = min(y + 1, h - 1);
     const float s = (float)img[y * w + x] + (float)img[y * w + x1] + (float)img[y1 * w + x] + (float)img[y1 * w + x1];
     box[y * w + x] = 0.25f * s - 128.0f;
+  }
+}
+
+// Even / odd column planes of the (I - 128) reference image:
+// out[p][y][i] = ref[y][2i + p]  (0 past the right edge).
+__global__ void k_deinterleave(const float* __restrict__ ref, int w, int h, int half_w, float* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= half_w || y >= h) return;
+  for (int p = 0; p < 2; ++p) {
+    const int x = 2 * i + p;
+    out[((size_t)p * h + y) * half_w + i] = x < w ? ref[(size_t)y * w + x] : 0.f;
   }
 }
 
@@ -856,8 +942,13 @@ cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const
   const int threads = 128;
   const int blocks = (n + threads - 1) / threads;
   if (blocks == 0) return cudaSuccess;
-  k_eval_hyps<<<blocks, threads, pcache_bytes(J.num_src, threads), st>>>(J, mode, n, px, py, inv, normals, cost,
-                                                                          support, view_cost);
+  const size_t sm = pcache_bytes(J.num_src, threads);
+  if (J.patch_half == 5)
+    k_eval_hyps<5><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+  else if (J.patch_half == 3)
+    k_eval_hyps<3><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+  else
+    k_eval_hyps<0><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
   return cudaGetLastError();
 }
 
@@ -865,20 +956,38 @@ static dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h +
 
 cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st) {
   const dim3 b(32, 4);
-  k_plane_init<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(J, seed_depth, seed_grid, seed_gx);
+  const size_t sm = pcache_bytes(J.num_src, 128);
+  if (J.patch_half == 5)
+    k_plane_init<5><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+  else if (J.patch_half == 3)
+    k_plane_init<3><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+  else
+    k_plane_init<0><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
   return cudaGetLastError();
 }
 
 cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters, cudaStream_t st) {
   const dim3 b(32, 4);
   const dim3 g((J.w + 63) / 64, (J.h + 3) / 4);
-  k_plane_sweep<<<g, b, pcache_bytes(J.num_src, 128), st>>>(J, color, iter, num_iters);
+  const size_t sm = pcache_bytes(J.num_src, 128);
+  if (J.patch_half == 5)
+    k_plane_sweep<5><<<g, b, sm, st>>>(J, color, iter, num_iters);
+  else if (J.patch_half == 3)
+    k_plane_sweep<3><<<g, b, sm, st>>>(J, color, iter, num_iters);
+  else
+    k_plane_sweep<0><<<g, b, sm, st>>>(J, color, iter, num_iters);
   return cudaGetLastError();
 }
 
 cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st) {
   const dim3 b(32, 4);
-  k_plane_refine<<<grid2d(J.w, J.h, b), b, pcache_bytes(J.num_src, 128), st>>>(J, inv_per_px, iters);
+  const size_t sm = pcache_bytes(J.num_src, 128);
+  if (J.patch_half == 5)
+    k_plane_refine<5><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+  else if (J.patch_half == 3)
+    k_plane_refine<3><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+  else
+    k_plane_refine<0><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
   return cudaGetLastError();
 }
 
@@ -957,6 +1066,12 @@ cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const u
   if (n <= 0) return cudaSuccess;
   k_ncc_windows<<<(n + 127) / 128, 128, 0, st>>>(ref, ref_w, ref_h, src, src_w, src_h, patch_size, n, win, valid, ncc,
                                                  weak, samples);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, float* out, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_deinterleave<<<grid2d(half_w, h, b), b, 0, st>>>(ref, w, h, half_w, out);
   return cudaGetLastError();
 }
 

@@ -318,3 +318,30 @@ def test_contract_violations(mvs):
     cfg2.min_depth_m, cfg2.max_depth_m = 0.9, 0.5
     dm = mvs.PatchMatchStereo(gpu_views(mvs, d), cfg2)
     assert dm.filled == 0 and np.isnan(dm.depth).all()
+
+
+@pytest.mark.parametrize("patch", [11, 7, 9])
+def test_sweep_costs_match_independent_evaluation(mvs, patch):
+    """The red-black sweep reads the reference window from its shared-memory
+    tile (window sizes 7 and 11) or from global memory (other sizes); the
+    cost it stores for each pixel must equal an independent evaluation of the
+    pixel's final hypothesis through recon_mvs_evaluate."""
+    import synthetic as S
+
+    sc = S.sphere_on_backdrop(width=200, height=150, f=190.0, num_sources=4, seed=12)
+    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    cfg = mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=2, patch_size=patch)
+    opts = mvs.Options(mode=mvs.MODE_PLANE, refine=0, best_k=3)
+    dm = mvs.PatchMatchStereo(va, cfg, options=opts)
+    ok = np.isfinite(dm.depth) & (dm.cost < 1e29)
+    ys, xs = np.nonzero(ok)
+    rng = np.random.default_rng(1)
+    pick = rng.choice(len(xs), 3000, replace=False)
+    px, py = xs[pick], ys[pick]
+    inv = 1.0 / dm.depth[py, px].astype(np.float64)
+    cost, _ = mvs.Evaluate(va, cfg, opts, px, py, inv, dm.normal[py, px])
+    d = np.abs(cost.astype(np.float64) - dm.cost[py, px])
+    print(f"patch {patch}: max |d| {d.max():.2e}, p99 {np.quantile(d, 0.99):.2e}")
+    assert np.quantile(d, 0.99) < 2e-5 and d.max() < 1e-3
