@@ -134,7 +134,10 @@ typedef struct recon_mvs_options {
   int32_t refine;     /* plane mode: 1 = golden-section inverse-depth refinement after the sweeps */
   uint64_t seed;      /* plane mode random stream */
   int32_t device;     /* CUDA device ordinal */
-  int32_t reserved[7];
+  int32_t sampling;   /* plane mode: 0 = pixel-centre windows; 1 = the reference's convention
+                         (window samples at x + 0.5 + dx read with index == coordinate, i.e. a
+                         2x2-box reference window and unshifted source coordinates) */
+  int32_t reserved[6];
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list

@@ -1076,7 +1076,8 @@ static int sample_centre(const uint8_t* img, int w, int h, double cu, double cv,
 }
 
 orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32_t best_k,
-                                int32_t x, int32_t y, double inv_depth, const double n[3]) {
+                                int32_t x, int32_t y, double inv_depth, const double n[3],
+                                int32_t half_pixel) {
   orc_plane_result res;
   memset(&res, 0, sizeof(res));
   res.cost = 1e30;
@@ -1120,8 +1121,13 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
     for (int dy = -half; dy <= half; ++dy) {
       for (int dx = -half; dx <= half; ++dx) {
         const int rx = x + dx, ry = y + dy;
-        if (rx < 0 || ry < 0 || rx > v->ref_w - 1 || ry > v->ref_h - 1) continue;
-        const double vr = v->ref[(size_t)ry * v->ref_w + rx];
+        double vr = 0.0;
+        if (half_pixel) {
+          if (!orc_sample_bilinear(v->ref, v->ref_w, v->ref_h, rx + 0.5, ry + 0.5, &vr)) continue;
+        } else {
+          if (rx < 0 || ry < 0 || rx > v->ref_w - 1 || ry > v->ref_h - 1) continue;
+          vr = v->ref[(size_t)ry * v->ref_w + rx];
+        }
         const double rp[3] = {(rx + 0.5 - kr->cx) / kr->fx, (ry + 0.5 - kr->cy) / kr->fy, 1.0};
         const double nd = n[0] * rp[0] + n[1] * rp[1] + n[2] * rp[2];
         if (!(nd < 0.0)) continue;
@@ -1134,7 +1140,11 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
         const double su = ks->fx * (Xs[0] / Xs[2]) + ks->cx;
         const double sv = ks->fy * (Xs[1] / Xs[2]) + ks->cy;
         double vs = 0.0;
-        if (!sample_centre(v->src[k], v->src_w[k], v->src_h[k], su, sv, &vs)) continue;
+        if (half_pixel) {
+          if (!orc_sample_bilinear(v->src[k], v->src_w[k], v->src_h[k], su, sv, &vs)) continue;
+        } else if (!sample_centre(v->src[k], v->src_w[k], v->src_h[k], su, sv, &vs)) {
+          continue;
+        }
         sr += vr;
         ss += vs;
         srr += vr * vr;
@@ -1180,9 +1190,9 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
 void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, int32_t n,
                      const int32_t* px, const int32_t* py, const double* inv,
                      const double* normals, double* out_cost, int32_t* out_valid_views,
-                     double* out_view_cost) {
+                     double* out_view_cost, int32_t half_pixel) {
   for (int32_t i = 0; i < n; ++i) {
-    const orc_plane_result r = orc_plane_cost(v, cfg, best_k, px[i], py[i], inv[i], &normals[3 * i]);
+    const orc_plane_result r = orc_plane_cost(v, cfg, best_k, px[i], py[i], inv[i], &normals[3 * i], half_pixel);
     out_cost[i] = r.cost;
     out_valid_views[i] = r.valid_views;
     if (out_view_cost)

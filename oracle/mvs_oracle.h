@@ -199,12 +199,17 @@ typedef struct orc_plane_result {
   double view_cost[32];
   int32_t view_valid[32];
 } orc_plane_result;
+/* half_pixel = 1 selects the reference's sampling convention instead: the
+ * reference window sampled at (x+0.5+dx, y+0.5+dy) with index == coordinate
+ * (SampleBilinear, patchmatch_stereo.cpp:78-100) and source coordinates used
+ * as indices directly. */
 orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32_t best_k,
-                                int32_t x, int32_t y, double inv_depth, const double n[3]);
+                                int32_t x, int32_t y, double inv_depth, const double n[3],
+                                int32_t half_pixel);
 void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, int32_t n,
                      const int32_t* px, const int32_t* py, const double* inv,
                      const double* normals, double* out_cost, int32_t* out_valid_views,
-                     double* out_view_cost);
+                     double* out_view_cost, int32_t half_pixel);
 
 /* Geometric consistency (spec: shaders/vulkan/recon_mvs_consistency.comp:94-140
  * with the strict transform of shaders/common/gpu_algo.h:537-538, plus a

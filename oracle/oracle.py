@@ -212,7 +212,7 @@ def load(which: str = "oracle") -> "Checker":
         lib.orc_fuse_depth_maps.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
                                             P, C.c_int64, C.POINTER(C.c_int64), d, d, C.POINTER(C.c_float),
                                             C.POINTER(C.c_uint32)]
-        lib.orc_plane_costs.argtypes = [V, P, C.c_int32, C.c_int32, i32, i32, d, d, d, i32, d]
+        lib.orc_plane_costs.argtypes = [V, P, C.c_int32, C.c_int32, i32, i32, d, d, d, i32, d, C.c_int32]
         lib.orc_geo_consistency.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
                                             C.c_int32, C.POINTER(ConsistencyParams), C.POINTER(C.c_uint8),
                                             C.POINTER(C.c_uint8)]
@@ -359,7 +359,7 @@ class Checker:
                                    _ptr(bc, C.c_double), _ptr(wr, C.c_int32))
         return bi, bc, wr
 
-    def plane_costs(self, vs: ViewSet, cfg: Config, best_k, px, py, inv, normals):
+    def plane_costs(self, vs: ViewSet, cfg: Config, best_k, px, py, inv, normals, half_pixel=0):
         px = np.ascontiguousarray(px, np.int32)
         py = np.ascontiguousarray(py, np.int32)
         inv = np.ascontiguousarray(inv, np.float64)
@@ -370,7 +370,8 @@ class Checker:
         view_cost = np.zeros((n, len(vs.srcs)), np.float64)
         self.lib.orc_plane_costs(C.byref(vs.struct), C.byref(cfg), best_k, n, _ptr(px, C.c_int32),
                                  _ptr(py, C.c_int32), _ptr(inv, C.c_double), _ptr(nrm, C.c_double),
-                                 _ptr(cost, C.c_double), _ptr(vv, C.c_int32), _ptr(view_cost, C.c_double))
+                                 _ptr(cost, C.c_double), _ptr(vv, C.c_int32), _ptr(view_cost, C.c_double),
+                                 int(half_pixel))
         return cost, vv, view_cost
 
     def undistort(self, img, intr):

@@ -161,8 +161,14 @@ struct Job {
   double rk1, rk2, rk3, rp1, rp2;
   const float* ref;      // (I - 128), row-major w x h
   const float* ref_box;  // compat: 2x2 box average of (I - 128), (w-1) x (h-1) used
-  const float* ref_de;   // plane mode: even / odd column planes of ref, [2][h][ref_half_w]
+  const float* ref_de;   // plane mode: even / odd column planes of pref, [2][h][ref_half_w]
   int ref_half_w;
+  // plane mode sampling convention: 0 = pixel centres (reference window =
+  // pixels, source index = coordinate - 0.5); 1 = the reference's own
+  // (window at x + 0.5 + dx with index == coordinate, i.e. the 2x2 box image,
+  // source index == coordinate)
+  int half_pixel;
+  const float* pref;     // the plane-mode reference window image: ref or ref_box
   const SrcView* src;    // num_src entries (device memory)
   // plane-mode state
   float4* hyp;   // {rho, nx, ny, nz}

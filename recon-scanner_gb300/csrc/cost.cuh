@@ -201,13 +201,13 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
   const float umin = (float)(-iu), vmin = (float)(-iv);
   for (int dy = -h; dy <= h; ++dy) {
     const int ry = y + dy;
-    if (!kFull && (ry < 0 || ry >= J.h)) continue;
+    if (!kFull && (ry < 0 || ry > J.h - 1 - J.half_pixel)) continue;
     const float fdy = (float)dy;
     float den = fmaf(fdy, c1, 1.0f - (float)h * c0);
     float nu = fmaf(fdy, A1, -(float)h * A0);
     float nv = fmaf(fdy, B1, -(float)h * B0);
     float nr = hp.kappa + fdy * hp.ey - (float)h * hp.ex;
-    const float* rrow = J.ref + (size_t)ry * J.w + x;
+    const float* rrow = J.pref + (size_t)ry * J.w + x;
     float r_s = 0.f, r_ss = 0.f, r_rs = 0.f, r_r = 0.f, r_rr = 0.f, r_n = 0.f;
 #pragma unroll 4
     for (int dx = -h; dx <= h; ++dx) {
@@ -217,7 +217,7 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
       bool ok = true;
       if (!kFull) {
         const int rx = x + dx;
-        ok = rx >= 0 && rx < J.w && den > 0.0f && nr < 0.0f && tu >= umin && tu <= umax && tv >= vmin &&
+        ok = rx >= 0 && rx <= J.w - 1 - J.half_pixel && den > 0.0f && nr < 0.0f && tu >= umin && tu <= umax && tv >= vmin &&
              tv <= vmax;
       }
       if (ok) {
@@ -379,8 +379,9 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   // pixel-centre convention: index coordinate = coordinate - 0.5
   int iu, iv;
   float fu, fv;
-  ff_floor_frac(ff_add(u0, ff_make(-0.5f)), &iu, &fu);
-  ff_floor_frac(ff_add(v0, ff_make(-0.5f)), &iv, &fv);
+  const float shift = J.half_pixel ? 0.0f : -0.5f;
+  ff_floor_frac(ff_add(u0, ff_make(shift)), &iu, &fu);
+  ff_floor_frac(ff_add(v0, ff_make(shift)), &iv, &fv);
   const int h = H > 0 ? H : J.patch_half;
   const float fh = (float)h;
   // fast path: the four corners (hence, by convexity, the whole window)

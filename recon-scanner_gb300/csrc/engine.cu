@@ -357,16 +357,17 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   const void* ref_dev = upload_image(C, v->ref_gray, D.w, D.h, undistort ? &rk : nullptr, D.ref_u8, ref_und, &ref_f32);
   D.ref.alloc((size_t)D.w * D.h);
   const bool compat = !plane;
-  if (compat) D.ref_box.alloc((size_t)D.w * D.h);
+  const bool want_box = compat || C.opts.sampling == 1;
+  if (want_box) D.ref_box.alloc((size_t)D.w * D.h);
   if (ref_f32)
-    CK(launch_prep_ref_f32((const float*)ref_dev, D.w, D.h, D.ref.p, compat ? D.ref_box.p : nullptr, C.stream));
+    CK(launch_prep_ref_f32((const float*)ref_dev, D.w, D.h, D.ref.p, want_box ? D.ref_box.p : nullptr, C.stream));
   else
-    CK(launch_prep_ref((const uint8_t*)ref_dev, D.w, D.h, D.ref.p, compat ? D.ref_box.p : nullptr, C.stream));
+    CK(launch_prep_ref((const uint8_t*)ref_dev, D.w, D.h, D.ref.p, want_box ? D.ref_box.p : nullptr, C.stream));
   if (undistort) rk.k1 = rk.k2 = rk.k3 = rk.p1 = rk.p2 = 0.0;
   const int half_w = (D.w + 1) / 2;
   if (plane) {
     D.ref_de.alloc((size_t)2 * half_w * D.h);
-    CK(launch_deinterleave(D.ref.p, D.w, D.h, half_w, D.ref_de.p, C.stream));
+    CK(launch_deinterleave(C.opts.sampling == 1 ? D.ref_box.p : D.ref.p, D.w, D.h, half_w, D.ref_de.p, C.stream));
   }
 
   // ---- sources ----
@@ -449,6 +450,8 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   J.ref_box = D.ref_box.p;
   J.ref_de = D.ref_de.p;
   J.ref_half_w = half_w;
+  J.half_pixel = (plane && C.opts.sampling == 1) ? 1 : 0;
+  J.pref = J.half_pixel ? D.ref_box.p : D.ref.p;
   J.src = D.src_table.p;
   J.dinv_min = inv_min;
   J.dinv_max = inv_max;

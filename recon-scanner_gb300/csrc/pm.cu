@@ -168,8 +168,8 @@ __global__ void k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, 
     const RefWindow rw = ref_window(J, x, y, true);
     r = eval_compat_hyp(J, pc, x, y, inv[i], rw, vc);
   } else {
-    const RefWindow rw = ref_window(J, x, y, false);
-    const GlobalRef ref{J.ref, J.w, x, y};
+    const RefWindow rw = ref_window(J, x, y, J.half_pixel);
+    const GlobalRef ref{J.pref, J.w, x, y};
     r = eval_plane_hyp<H>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
                           rw, ref, vc);
   }
@@ -255,8 +255,8 @@ __global__ void k_plane_init(Job J, const float* __restrict__ seed_depth, int se
       nz = -1.f;
     }
   }
-  const RefWindow rw = ref_window(J, x, y, false);
-  const GlobalRef ref{J.ref, J.w, x, y};
+  const RefWindow rw = ref_window(J, x, y, J.half_pixel);
+  const GlobalRef ref{J.pref, J.w, x, y};
   const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
   J.hyp[idx] = make_float4(rho, nx, ny, nz);
   J.cost[idx] = c.cost;
@@ -284,8 +284,8 @@ __device__ __forceinline__ void plane_candidate_transfer(const float4 hn, float 
 template <int H>
 __device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t, int x, int y) {
   RefWindow rw;
-  rw.full = x >= H && y >= H && x + H <= J.w - 1 && y + H <= J.h - 1;
-  if (!rw.full) return ref_window(J, x, y, false);
+  rw.full = x >= H && y >= H && x + H <= J.w - 1 - J.half_pixel && y + H <= J.h - 1 - J.half_pixel;
+  if (!rw.full) return ref_window(J, x, y, J.half_pixel);
   float s = 0.f;
 #pragma unroll 1
   for (int dy = -H; dy <= H; ++dy) {
@@ -348,12 +348,12 @@ __global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int it
     ref = TileRef{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
                   (int)threadIdx.x, parity, (int)threadIdx.y};
   else
-    ref = GlobalRef{J.ref, J.w, x, y};
+    ref = GlobalRef{J.pref, J.w, x, y};
   RefWindow rw;
   if constexpr (H > 0)
     rw = tile_window<H>(J, ref, x, y);
   else
-    rw = ref_window(J, x, y, false);
+    rw = ref_window(J, x, y, J.half_pixel);
   float4 cur = J.hyp[idx];
   float cur_cost = J.cost[idx];
   int cur_sup = J.support[idx];
@@ -752,8 +752,8 @@ __global__ void k_plane_refine(Job J, double inv_per_px, int subpixel_iterations
   if (!(c0 < 1e29f)) return;
   float rx, ry;
   fill_pcache(J, pc, x, y, &rx, &ry);
-  const RefWindow rw = ref_window(J, x, y, false);
-  const GlobalRef ref{J.ref, J.w, x, y};
+  const RefWindow rw = ref_window(J, x, y, J.half_pixel);
+  const GlobalRef ref{J.pref, J.w, x, y};
   auto eval = [&](float v) -> HypCost {
     return eval_plane_hyp<H>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
   };

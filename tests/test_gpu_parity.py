@@ -104,14 +104,15 @@ def test_plane_cost_matches_fp64_oracle(mvs, orc):
     px, py, inv, nrm = plane_hypotheses(sc, 4000, 7)
     cfg_d = dict(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, patch_size=11)
     vs_o = O.ViewSet(imgs[0], imgs[1:], cams[0], cams[1:])
-    for best_k in (0, 2):
-        want, want_sup, want_view = orc.plane_costs(vs_o, O.make_config(**cfg_d), best_k, px, py, inv, nrm)
+    for best_k, sampling in ((0, 0), (2, 0), (2, 1)):
+        want, want_sup, want_view = orc.plane_costs(vs_o, O.make_config(**cfg_d), best_k, px, py, inv, nrm,
+                                                    half_pixel=sampling)
         for storage in (mvs.STORAGE_FP32, mvs.STORAGE_FP16):
-            opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=best_k, storage=storage)
+            opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=best_k, storage=storage, sampling=sampling)
             va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
             got, sup, view = mvs.Evaluate(va, mvs.MvsConfig(**cfg_d), opts, px, py, inv, nrm.astype(np.float32),
                                           per_view=True)
-            assert_costs_close(got, want, f"plane best_k={best_k} storage={storage}")
+            assert_costs_close(got, want, f"plane best_k={best_k} storage={storage} sampling={sampling}")
             assert_costs_close(view.ravel(), want_view.ravel(), "per-view")
 
 
