@@ -277,7 +277,7 @@ def run_gpu(args):
     views = views_of(M, sc)
     cfg = config_of(M, sc)
     opts = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if args.fp16 else M.STORAGE_FP32,
-                     device=local, refine=1)
+                     device=local, refine=1, prefilter=int(args.prefilter), sampling=args.sampling)
     eng = M.Engine(opts)
     job = eng.stage(views, cfg, undistort=True)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
@@ -353,7 +353,8 @@ def run_gpu(args):
             "config": {"workload": f"{'tabletop' if WORKLOAD == 'c2' else 'sphere'} {W}x{H}, {S_SRC} sources, "
                                    f"{K}x{K}, {ITERS} iterations, "
                                    f"plane mode, best_k={args.best_k}, golden-section refine",
-                       "storage": "fp16" if args.fp16 else "fp32",
+                       "storage": "fp16" if args.fp16 else "fp32", "prefilter": bool(args.prefilter),
+                       "sampling": args.sampling,
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
@@ -385,6 +386,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--best-k", type=int, default=4)
     ap.add_argument("--fp16", action="store_true")
+    ap.add_argument("--prefilter", action="store_true", help="3x3 binomial pre-filter at staging")
+    ap.add_argument("--sampling", type=int, default=0, help="0 pixel-centre windows, 1 the reference's convention")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "small"])

@@ -137,7 +137,9 @@ typedef struct recon_mvs_options {
   int32_t sampling;   /* plane mode: 0 = pixel-centre windows; 1 = the reference's convention
                          (window samples at x + 0.5 + dx read with index == coordinate, i.e. a
                          2x2-box reference window and unshifted source coordinates) */
-  int32_t reserved[6];
+  int32_t prefilter;  /* 1 = smooth every image with a 3x3 binomial ([1 2 1]/4 each way) when it is
+                         staged: a shift-free low-pass that removes aliasing noise symmetrically */
+  int32_t reserved[5];
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list

@@ -386,20 +386,31 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const float fh = (float)h;
   // fast path: the four corners (hence, by convexity, the whole window)
   // inside the source, in front of it, and on the camera side of the plane
-  bool full = rw.full;
-  if (full) {
+  // The four corners decide the window: all inside (and in front of the
+  // source, on the camera side of the plane) -> every sample is valid, by
+  // convexity of the projective image of the window; all beyond one image
+  // edge -> no sample is valid and the view is invalid without sampling.
+  bool full = rw.full, front = true;
+  float umin_c = 3.4e38f, umax_c = -3.4e38f, vmin_c = 3.4e38f, vmax_c = -3.4e38f;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float dx = (c & 1) ? fh : -fh, dy = (c & 2) ? fh : -fh;
-      const float den = fmaf(dx, c0, fmaf(dy, c1, 1.0f));
-      const float rd = rcp_approx(den);
-      const float tu = fu + fmaf(dx, A0, dy * A1) * rd;
-      const float tv = fv + fmaf(dx, B0, dy * B1) * rd;
-      const float nr = hp.kappa + dx * hp.ex + dy * hp.ey;
-      full = full && den > 0.0f && nr < 0.0f && tu >= (float)(-iu) + 0.001f && tu <= (float)(S.w - 1 - iu) - 0.001f &&
-             tv >= (float)(-iv) + 0.001f && tv <= (float)(S.h - 1 - iv) - 0.001f;
-    }
+  for (int c = 0; c < 4; ++c) {
+    const float dx = (c & 1) ? fh : -fh, dy = (c & 2) ? fh : -fh;
+    const float den = fmaf(dx, c0, fmaf(dy, c1, 1.0f));
+    const float rd = rcp_approx(den);
+    const float tu = fu + fmaf(dx, A0, dy * A1) * rd;
+    const float tv = fv + fmaf(dx, B0, dy * B1) * rd;
+    const float nr = hp.kappa + dx * hp.ex + dy * hp.ey;
+    front = front && den > 0.0f && nr < 0.0f;
+    umin_c = fminf(umin_c, tu);
+    umax_c = fmaxf(umax_c, tu);
+    vmin_c = fminf(vmin_c, tv);
+    vmax_c = fmaxf(vmax_c, tv);
   }
+  const float ulo = (float)(-iu), uhi = (float)(S.w - 1 - iu), vlo = (float)(-iv), vhi = (float)(S.h - 1 - iv);
+  full = full && front && umin_c >= ulo + 0.001f && umax_c <= uhi - 0.001f && vmin_c >= vlo + 0.001f &&
+         vmax_c <= vhi - 0.001f;
+  const bool outside = front && (umax_c < ulo - 0.001f || umin_c > uhi + 0.001f || vmax_c < vlo - 0.001f ||
+                                 vmin_c > vhi + 0.001f);
   // source centring value: the sample at the window centre (clamped read)
   const float sc = bilinear(S.tex, (float)iu, (float)iv, fu, fv);
   float acc[5], n;
@@ -412,6 +423,7 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
       plane_window<true>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
+  if (outside) return bad;
   plane_window<false>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
 }

@@ -318,15 +318,27 @@ static const void* upload_image(Context& C, const uint8_t* host, int w, int h, c
                                 DevArray<uint8_t>& u8, DevArray<float>& f32, bool* is_f32) {
   u8.alloc((size_t)w * h);
   CK(cudaMemcpyAsync(u8.p, host, (size_t)w * h, cudaMemcpyHostToDevice, C.stream));
+  const void* out = u8.p;
+  *is_f32 = false;
   if (und && distorted(*und)) {
     f32.alloc((size_t)w * h);
     UndistortCam K{und->fx, und->fy, und->cx, und->cy, und->k1, und->k2, und->k3, und->p1, und->p2};
     CK(launch_undistort(u8.p, w, h, K, f32.p, C.stream));
     *is_f32 = true;
-    return f32.p;
+    out = f32.p;
   }
-  *is_f32 = false;
-  return u8.p;
+  if (C.opts.prefilter) {
+    DevArray<float> tmp;
+    tmp.alloc((size_t)w * h);
+    CK(launch_binomial(*is_f32 ? nullptr : u8.p, *is_f32 ? f32.p : nullptr, w, h, tmp.p, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    f32.alloc((size_t)w * h);
+    CK(cudaMemcpyAsync(f32.p, tmp.p, (size_t)w * h * sizeof(float), cudaMemcpyDeviceToDevice, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    *is_f32 = true;
+    out = f32.p;
+  }
+  return out;
 }
 
 static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,

@@ -272,6 +272,31 @@ __global__ void k_undistort(const uint8_t* __restrict__ img, int w, int h, Undis
 }
 
 // ---------------------------------------------------------------------------
+// 3x3 binomial low-pass ([1 2 1]/4 in each direction, edge-clamped): the
+// optional staging pre-filter.  Input u8 (in_u8) or float (in_f32).
+// ---------------------------------------------------------------------------
+__global__ void k_binomial(const uint8_t* __restrict__ in_u8, const float* __restrict__ in_f32, int w, int h,
+                           float* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  float acc = 0.f;
+#pragma unroll
+  for (int j = -1; j <= 1; ++j) {
+    const int yy = min(max(y + j, 0), h - 1);
+    const float wy = j == 0 ? 0.5f : 0.25f;
+#pragma unroll
+    for (int i = -1; i <= 1; ++i) {
+      const int xx = min(max(x + i, 0), w - 1);
+      const float wx = i == 0 ? 0.5f : 0.25f;
+      const float v = in_u8 ? (float)in_u8[(size_t)yy * w + xx] : in_f32[(size_t)yy * w + xx];
+      acc = fmaf(wx * wy, v, acc);
+    }
+  }
+  out[(size_t)y * w + x] = acc;
+}
+
+// ---------------------------------------------------------------------------
 // exclusive scan of uint32 (three-phase, recursive over block sums)
 // ---------------------------------------------------------------------------
 constexpr int kScanBlock = 1024;
@@ -381,6 +406,12 @@ cudaError_t launch_consistency(const ConsistencyRef& R, const ConsistencySrc* S,
   const dim3 b(32, 8);
   const float r2 = reproj_px_max * reproj_px_max;
   k_consistency<<<g2(R.w, R.h, b), b, 0, st>>>(R, S, num_src, rel_max, r2, min_views, count, keep);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_binomial(const uint8_t* in_u8, const float* in_f32, int w, int h, float* out, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_binomial<<<g2(w, h, b), b, 0, st>>>(in_u8, in_f32, w, h, out);
   return cudaGetLastError();
 }
 

@@ -97,6 +97,7 @@ cudaError_t launch_fuse_reduce(unsigned int nvox, const unsigned int* voffset, c
                                unsigned int* ocount, cudaStream_t st);
 cudaError_t launch_consistency(const ConsistencyRef& R, const ConsistencySrc* S, int num_src, float rel_max,
                                float reproj_px_max, int min_views, uint8_t* count, uint8_t* keep, cudaStream_t st);
+cudaError_t launch_binomial(const uint8_t* in_u8, const float* in_f32, int w, int h, float* out, cudaStream_t st);
 cudaError_t launch_undistort(const uint8_t* img, int w, int h, const UndistortCam& K, float* out, cudaStream_t st);
 
 int64_t scan_scratch_elems(int64_t n);

@@ -152,7 +152,7 @@ __device__ HypCost eval_compat_hyp(const Job& J, const PCache& pc, int x, int y,
 // batch evaluation of given hypotheses (parity instrument, adjoint driver)
 // ---------------------------------------------------------------------------
 template <int H>
-__global__ void k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
+__global__ void __launch_bounds__(128, 4) k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
                             const double* __restrict__ inv, const float* __restrict__ normals, float* out_cost,
                             int* out_support, float* out_view_cost) {
   extern __shared__ float2 smem[];
@@ -230,7 +230,7 @@ __device__ __forceinline__ Rng pixel_rng(const Job& J, int idx, int iter, int sa
 }
 
 template <int H>
-__global__ void k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
+__global__ void __launch_bounds__(128, 4) k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -739,7 +739,7 @@ __global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per
 // the pixel's own plane normal over +-1 px of disparity, the reference's
 // refinement schedule applied to the plane cost.
 template <int H>
-__global__ void k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
+__global__ void __launch_bounds__(128, 4) k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
