@@ -277,7 +277,8 @@ def run_gpu(args):
     views = views_of(M, sc)
     cfg = config_of(M, sc)
     opts = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if args.fp16 else M.STORAGE_FP32,
-                     device=local, refine=1, prefilter=int(args.prefilter), sampling=args.sampling)
+                     device=local, refine=1, prefilter=int(args.prefilter), sampling=args.sampling,
+                     interp=args.interp)
     eng = M.Engine(opts)
     job = eng.stage(views, cfg, undistort=True)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
@@ -354,7 +355,7 @@ def run_gpu(args):
                                    f"{K}x{K}, {ITERS} iterations, "
                                    f"plane mode, best_k={args.best_k}, golden-section refine",
                        "storage": "fp16" if args.fp16 else "fp32", "prefilter": bool(args.prefilter),
-                       "sampling": args.sampling,
+                       "sampling": args.sampling, "interp": "texture-unit" if args.interp else "exact fp32",
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
@@ -388,6 +389,7 @@ def main():
     ap.add_argument("--fp16", action="store_true")
     ap.add_argument("--prefilter", action="store_true", help="3x3 binomial pre-filter at staging")
     ap.add_argument("--sampling", type=int, default=0, help="0 pixel-centre windows, 1 the reference's convention")
+    ap.add_argument("--interp", type=int, default=0, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "small"])

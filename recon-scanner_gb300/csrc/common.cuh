@@ -136,7 +136,8 @@ struct Rng {
 // One source view of one job.  A, b map reference-camera points to this
 // camera: X_s = A X_r + b (composed in FP64 on the host).
 struct SrcView {
-  cudaTextureObject_t tex;  // (I - 128), FP32 or FP16, clamp, point filter
+  cudaTextureObject_t tex;      // (I - 128), FP32 or FP16, clamp, point filter (gather)
+  cudaTextureObject_t tex_lin;  // the same array with hardware bilinear filtering
   int w, h;
   float fx, fy, cx, cy;
   ff ffx, ffy, fcx, fcy;
@@ -168,6 +169,9 @@ struct Job {
   // (window at x + 0.5 + dx with index == coordinate, i.e. the 2x2 box image,
   // source index == coordinate)
   int half_pixel;
+  // plane mode interpolation: 0 = exact FP32 bilinear from a 2x2 gather;
+  // 1 = the texture unit's bilinear filter (8-bit fixed-point weights)
+  int hw_interp;
   const float* pref;     // the plane-mode reference window image: ref or ref_box
   const SrcView* src;    // num_src entries (device memory)
   // plane-mode state

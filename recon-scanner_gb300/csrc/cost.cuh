@@ -190,7 +190,7 @@ __device__ __forceinline__ bool make_plane_hyp(const Job& J, float rx, float ry,
   return true;
 }
 
-template <bool kFull>
+template <bool kFull, bool kHw>
 __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int x, int y, int iu, int iv, float fu,
                                              float fv, float A0, float A1, float B0, float B1, float c0, float c1,
                                              const PlaneHyp& hp, float rmean, float sc, float* acc, float* cnt) {
@@ -222,7 +222,8 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
       }
       if (ok) {
         const float flu = floorf(tu), flv = floorf(tv);
-        const float sv = bilinear(S.tex, bu + flu, bv + flv, tu - flu, tv - flv) - sc;
+        const float sv = (kHw ? tex2D<float>(S.tex_lin, bu + tu + 0.5f, bv + tv + 0.5f)
+                              : bilinear(S.tex, bu + flu, bv + flv, tu - flu, tv - flv)) - sc;
         const float rv = __ldg(rrow + dx) - rmean;
         r_s += sv;
         r_ss = fmaf(sv, sv, r_ss);
@@ -299,24 +300,31 @@ struct TileRef {
 // rounding (FMA pipe): m = t' + 1.5*2^23 rounds t' = t - 0.5 to the nearest
 // integer, i.e. floor(t); at exact ties the footprint shifts by one texel
 // with weight 1, which reads the same value (bilinear is continuous).
-template <int H, class Row>
-__device__ __forceinline__ void plane_row(cudaTextureObject_t tex, const Row& row, float& den, float& nu, float& nv,
-                                          float c0, float A0, float B0, float fum, float fvm, float gxo, float gyo,
-                                          float rmean, float sc, float& r_s, float& r_ss, float& r_rs) {
+template <int H, bool kHw, class Row>
+__device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Row& row,
+                                          float& den, float& nu, float& nv, float c0, float A0, float B0, float fum,
+                                          float fvm, float gxo, float gyo, float cuo, float cvo, float rmean, float sc,
+                                          float& r_s, float& r_ss, float& r_rs) {
   constexpr float kM = 12582912.0f;
 #pragma unroll
   for (int k = 0; k <= 2 * H; ++k) {
     const float rinv = rcp_approx(den);
-    const float tmu = fmaf(nu, rinv, fum);
-    const float tmv = fmaf(nv, rinv, fvm);
-    const float mu = __fadd_rn(tmu, kM), mv = __fadd_rn(tmv, kM);
-    const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
-    const float wu = __fadd_rn(__fsub_rn(tmu, flu), 0.5f);
-    const float wv = __fadd_rn(__fsub_rn(tmv, flv), 0.5f);
-    const float4 g = tex2Dgather<float4>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo), 0);
-    const float top = fmaf(wu, g.z - g.w, g.w);
-    const float bot = fmaf(wu, g.y - g.x, g.x);
-    const float sv = fmaf(wv, bot - top, top) - sc;
+    float sv;
+    if constexpr (kHw) {
+      // texture coordinate of index coordinate t: t + 0.5
+      sv = tex2D<float>(tex_lin, fmaf(nu, rinv, cuo), fmaf(nv, rinv, cvo)) - sc;
+    } else {
+      const float tmu = fmaf(nu, rinv, fum);
+      const float tmv = fmaf(nv, rinv, fvm);
+      const float mu = __fadd_rn(tmu, kM), mv = __fadd_rn(tmv, kM);
+      const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
+      const float wu = __fadd_rn(__fsub_rn(tmu, flu), 0.5f);
+      const float wv = __fadd_rn(__fsub_rn(tmv, flv), 0.5f);
+      const float4 g = tex2Dgather<float4>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo), 0);
+      const float top = fmaf(wu, g.z - g.w, g.w);
+      const float bot = fmaf(wu, g.y - g.x, g.x);
+      sv = fmaf(wv, bot - top, top) - sc;
+    }
     const float rv = ((k & 1) ? row.odd(k >> 1) : row.even(k >> 1)) - rmean;
     r_s += sv;
     r_ss = fmaf(sv, sv, r_ss);
@@ -327,13 +335,14 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, const Row& ro
   }
 }
 
-template <int H, class Ref>
-__device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, const Ref& ref, int iu, int iv, float fu,
-                                                  float fv, float A0, float A1, float B0, float B1, float c0, float c1,
-                                                  float rmean, float sc, float* acc) {
+template <int H, bool kHw, class Ref>
+__device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Ref& ref,
+                                                  int iu, int iv, float fu, float fv, float A0, float A1, float B0,
+                                                  float B1, float c0, float c1, float rmean, float sc, float* acc) {
   constexpr float kM = 12582912.0f;
   const float fum = fu - 0.5f, fvm = fv - 0.5f;
   const float gxo = ((float)iu + 1.0f) - kM, gyo = ((float)iv + 1.0f) - kM;
+  const float cuo = ((float)iu + 0.5f) + fu, cvo = ((float)iv + 0.5f) + fv;
   float ss = 0.f, sss = 0.f, srs = 0.f;
 #pragma unroll 1
   for (int dy = -H; dy <= H; ++dy) {
@@ -342,8 +351,8 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, const
     float nu = fmaf(fdy, A1, -(float)H * A0);
     float nv = fmaf(fdy, B1, -(float)H * B0);
     float r_s = 0.f, r_ss = 0.f, r_rs = 0.f;
-    plane_row<H>(tex, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, rmean, sc, r_s, r_ss,
-                 r_rs);
+    plane_row<H, kHw>(tex, tex_lin, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, cuo, cvo,
+                      rmean, sc, r_s, r_ss, r_rs);
     ss += r_s;
     sss += r_ss;
     srs += r_rs;
@@ -355,7 +364,7 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, const
 
 // H > 0: windows of 2H+1 known at compile time, reference samples through
 // `ref` on the fast path; H == 0: any window size (runtime loop).
-template <int H, class Ref>
+template <int H, bool kHw, class Ref>
 __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
                                                       const PlaneHyp& hp, const RefWindow& rw, const Ref& ref) {
   ViewResult bad{0.0f, 0};
@@ -412,19 +421,20 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const bool outside = front && (umax_c < ulo - 0.001f || umin_c > uhi + 0.001f || vmax_c < vlo - 0.001f ||
                                  vmin_c > vhi + 0.001f);
   // source centring value: the sample at the window centre (clamped read)
-  const float sc = bilinear(S.tex, (float)iu, (float)iv, fu, fv);
+  const float sc = kHw ? tex2D<float>(S.tex_lin, (float)iu + 0.5f + fu, (float)iv + 0.5f + fv)
+                      : bilinear(S.tex, (float)iu, (float)iv, fu, fv);
   float acc[5], n;
   const int K = 2 * h + 1;
   const int min_valid = J.min_valid;
   if (full) {
     if constexpr (H > 0)
-      plane_window_fast<H>(S.tex, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
+      plane_window_fast<H, kHw>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
     else
-      plane_window<true>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+      plane_window<true, kHw>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
   if (outside) return bad;
-  plane_window<false>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  plane_window<false, kHw>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
 }
 

@@ -113,8 +113,10 @@ struct PinnedBuf {
 struct Texture {
   cudaArray_t arr = nullptr;
   cudaTextureObject_t tex = 0;
+  cudaTextureObject_t tex_lin = 0;
   ~Texture() {
     if (tex) cudaDestroyTextureObject(tex);
+    if (tex_lin) cudaDestroyTextureObject(tex_lin);
     if (arr) cudaFreeArray(arr);
   }
 };
@@ -310,6 +312,8 @@ static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32,
   td.readMode = cudaReadModeElementType;
   td.normalizedCoords = 0;
   CK(cudaCreateTextureObject(&T.tex, &rd, &td, nullptr));
+  td.filterMode = cudaFilterModeLinear;
+  CK(cudaCreateTextureObject(&T.tex_lin, &rd, &td, nullptr));
 }
 
 // Upload an 8-bit host image (optionally undistorted) to a device buffer;
@@ -398,6 +402,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
     SrcView& S = D.host_src[k];
     std::memset(&S, 0, sizeof(S));
     S.tex = T->tex;
+    S.tex_lin = T->tex_lin;
     S.w = v->src_w[k];
     S.h = v->src_h[k];
     S.fx = (float)sk.fx;
@@ -463,6 +468,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   J.ref_de = D.ref_de.p;
   J.ref_half_w = half_w;
   J.half_pixel = (plane && C.opts.sampling == 1) ? 1 : 0;
+  J.hw_interp = (plane && C.opts.interp == 1) ? 1 : 0;
   J.pref = J.half_pixel ? D.ref_box.p : D.ref.p;
   J.src = D.src_table.p;
   J.dinv_min = inv_min;

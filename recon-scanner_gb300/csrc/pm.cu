@@ -83,7 +83,7 @@ __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int 
   return r;
 }
 
-template <int H, class Ref>
+template <int H, bool kHw, class Ref>
 __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
                                   float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
                                   int* nevals = nullptr) {
@@ -100,7 +100,7 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
   for (int s = 0; s < J.num_src; ++s) {
     ff P[3];
     pc.get(s, P);
-    const ViewResult v = eval_view_plane<H>(J, J.src[s], x, y, P, hp, rw, ref);
+    const ViewResult v = eval_view_plane<H, kHw>(J, J.src[s], x, y, P, hp, rw, ref);
     float c = kCostInf;
     if (v.valid) {
       c = 1.0f - v.ncc;
@@ -151,7 +151,7 @@ __device__ HypCost eval_compat_hyp(const Job& J, const PCache& pc, int x, int y,
 // ---------------------------------------------------------------------------
 // batch evaluation of given hypotheses (parity instrument, adjoint driver)
 // ---------------------------------------------------------------------------
-template <int H>
+template <int H, bool kHw>
 __global__ void __launch_bounds__(128, 4) k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
                             const double* __restrict__ inv, const float* __restrict__ normals, float* out_cost,
                             int* out_support, float* out_view_cost) {
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(128, 4) k_eval_hyps(Job J, int mode, int n, co
   } else {
     const RefWindow rw = ref_window(J, x, y, J.half_pixel);
     const GlobalRef ref{J.pref, J.w, x, y};
-    r = eval_plane_hyp<H>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
+    r = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
                           rw, ref, vc);
   }
   out_cost[i] = r.cost;
@@ -229,7 +229,7 @@ __device__ __forceinline__ Rng pixel_rng(const Job& J, int idx, int iter, int sa
   return g;
 }
 
-template <int H>
+template <int H, bool kHw>
 __global__ void __launch_bounds__(128, 4) k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(128, 4) k_plane_init(Job J, const float* __res
   }
   const RefWindow rw = ref_window(J, x, y, J.half_pixel);
   const GlobalRef ref{J.pref, J.w, x, y};
-  const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
+  const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
   J.hyp[idx] = make_float4(rho, nx, ny, nz);
   J.cost[idx] = c.cost;
   J.support[idx] = (uint8_t)min(c.support, 255);
@@ -314,7 +314,7 @@ __device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t,
 // same-colour pixels of each of 4 rows (64 columns); the reference rows it
 // reads (4 + 2H rows, the 64 columns +- 16) are staged once into shared
 // memory as even / odd column planes from the de-interleaved reference copy.
-template <int H>
+template <int H, bool kHw>
 __global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int iter, int num_iters) {
   extern __shared__ float2 smem[];
   constexpr int kRows = 4 + 2 * (H > 0 ? H : 1);
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int it
     plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
     if (!(rho > 0.f)) continue;
     if (rho == cur.x && hn.y == cur.y && hn.z == cur.z && hn.w == cur.w) continue;
-    const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int it
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
     }
-    const HypCost c = eval_plane_hyp<H>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, nx, ny, nz);
@@ -738,7 +738,7 @@ __global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per
 // Plane-mode refinement: golden-section search on the inverse depth along
 // the pixel's own plane normal over +-1 px of disparity, the reference's
 // refinement schedule applied to the plane cost.
-template <int H>
+template <int H, bool kHw>
 __global__ void __launch_bounds__(128, 4) k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
   extern __shared__ float2 smem[];
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine(Job J, double inv_per_p
   const RefWindow rw = ref_window(J, x, y, J.half_pixel);
   const GlobalRef ref{J.pref, J.w, x, y};
   auto eval = [&](float v) -> HypCost {
-    return eval_plane_hyp<H>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
+    return eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
   };
   float best_d = h0.x, best_c = c0;
   int best_s = J.support[idx];
@@ -943,12 +943,21 @@ cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const
   const int blocks = (n + threads - 1) / threads;
   if (blocks == 0) return cudaSuccess;
   const size_t sm = pcache_bytes(J.num_src, threads);
-  if (J.patch_half == 5)
-    k_eval_hyps<5><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-  else if (J.patch_half == 3)
-    k_eval_hyps<3><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-  else
-    k_eval_hyps<0><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+  if (J.hw_interp) {
+    if (J.patch_half == 5)
+      k_eval_hyps<5, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+    else if (J.patch_half == 3)
+      k_eval_hyps<3, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+    else
+      k_eval_hyps<0, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+  } else {
+    if (J.patch_half == 5)
+      k_eval_hyps<5, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+    else if (J.patch_half == 3)
+      k_eval_hyps<3, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+    else
+      k_eval_hyps<0, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+  }
   return cudaGetLastError();
 }
 
@@ -957,12 +966,21 @@ static dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h +
 cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st) {
   const dim3 b(32, 4);
   const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.patch_half == 5)
-    k_plane_init<5><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-  else if (J.patch_half == 3)
-    k_plane_init<3><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-  else
-    k_plane_init<0><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+  if (J.hw_interp) {
+    if (J.patch_half == 5)
+      k_plane_init<5, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+    else if (J.patch_half == 3)
+      k_plane_init<3, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+    else
+      k_plane_init<0, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+  } else {
+    if (J.patch_half == 5)
+      k_plane_init<5, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+    else if (J.patch_half == 3)
+      k_plane_init<3, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+    else
+      k_plane_init<0, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+  }
   return cudaGetLastError();
 }
 
@@ -970,24 +988,42 @@ cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters,
   const dim3 b(32, 4);
   const dim3 g((J.w + 63) / 64, (J.h + 3) / 4);
   const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.patch_half == 5)
-    k_plane_sweep<5><<<g, b, sm, st>>>(J, color, iter, num_iters);
-  else if (J.patch_half == 3)
-    k_plane_sweep<3><<<g, b, sm, st>>>(J, color, iter, num_iters);
-  else
-    k_plane_sweep<0><<<g, b, sm, st>>>(J, color, iter, num_iters);
+  if (J.hw_interp) {
+    if (J.patch_half == 5)
+      k_plane_sweep<5, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
+    else if (J.patch_half == 3)
+      k_plane_sweep<3, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
+    else
+      k_plane_sweep<0, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
+  } else {
+    if (J.patch_half == 5)
+      k_plane_sweep<5, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
+    else if (J.patch_half == 3)
+      k_plane_sweep<3, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
+    else
+      k_plane_sweep<0, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st) {
   const dim3 b(32, 4);
   const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.patch_half == 5)
-    k_plane_refine<5><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-  else if (J.patch_half == 3)
-    k_plane_refine<3><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-  else
-    k_plane_refine<0><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+  if (J.hw_interp) {
+    if (J.patch_half == 5)
+      k_plane_refine<5, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+    else if (J.patch_half == 3)
+      k_plane_refine<3, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+    else
+      k_plane_refine<0, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+  } else {
+    if (J.patch_half == 5)
+      k_plane_refine<5, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+    else if (J.patch_half == 3)
+      k_plane_refine<3, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+    else
+      k_plane_refine<0, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
+  }
   return cudaGetLastError();
 }
 
