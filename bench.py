@@ -8,6 +8,10 @@ plane, value-noise albedo with 10 % weak-texture patches), 11x11 windows,
 iterations, sub-pixel refinement, output.  Images are undistorted on the
 device when staged.
 
+  form   -- the chosen form: source images stored as FP16 textures, window
+            samples interpolated by the texture unit; the plain FP32 path
+            (FP32 textures, exact FP32 interpolation) is timed in the same
+            run and reported under "plain_fp32" with its depth agreement;
   value  -- depth maps/s with the staged inputs resident in HBM; each step
             is timed with CUDA events on the engine's stream and L2 is
             flushed (a 512 MiB write) between steps, outside the events;
@@ -263,6 +267,60 @@ def run_reference_arm(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 
+def time_form(M, views, cfg, opts, steps, warmup, flush, world, sampler=None):
+    """Stage once, run `warmup` untimed steps, then `steps` timed steps (CUDA
+    events on the engine stream; L2 flushed between steps, outside the
+    events).  Returns per-step ms, sweep ms, hypotheses, launches/step, map."""
+    import torch
+
+    eng = M.Engine(opts)
+    job = eng.stage(views, cfg, undistort=True)
+    for _ in range(warmup):
+        eng.run(job)
+        eng.synchronize()
+    step_ms, sweep_ms, hyps = [], [], []
+    launches = 0
+    barrier(world)
+    ctx = sampler if sampler is not None else _Null()
+    with ctx:
+        for _ in range(steps):
+            flush.random_(0, 255)
+            torch.cuda.synchronize()
+            h0 = eng.stats().hypotheses_evaluated
+            eng.run(job)
+            eng.synchronize()
+            st = eng.stats()
+            step_ms.append(st.last_run_ms)
+            sweep_ms.append(st.last_sweep_ms)
+            hyps.append(st.hypotheses_evaluated - h0)
+            launches = st.last_sweep_launches + 3  # init, refine, output
+    barrier(world)
+    dm = eng.download(job)
+    eng.release(job)
+    eng.close()
+    return step_ms, sweep_ms, hyps, launches, dm
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def accuracy(dm, truth):
+    import numpy as np
+
+    err = np.abs(dm.depth.astype(np.float64) - truth)
+    rel = err / truth
+    ok = np.isfinite(rel)
+    return {"filled": float(np.isfinite(dm.depth).mean()),
+            "median_rel_err": float(np.median(rel[ok])) if ok.any() else None,
+            "p95_rel_err": float(np.quantile(rel[ok], 0.95)) if ok.any() else None,
+            "median_abs_err_mm": float(np.median(err[ok]) * 1e3) if ok.any() else None}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -276,50 +334,47 @@ def run_gpu(args):
     sc = make_scene(f"cuda:{local}")
     views = views_of(M, sc)
     cfg = config_of(M, sc)
-    opts = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if args.fp16 else M.STORAGE_FP32,
-                     device=local, refine=1, prefilter=int(args.prefilter), sampling=args.sampling,
-                     interp=args.interp)
-    eng = M.Engine(opts)
-    job = eng.stage(views, cfg, undistort=True)
+    mk = lambda fp16, interp: M.Options(mode=M.MODE_PLANE, best_k=args.best_k,
+                                        storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local, refine=1,
+                                        prefilter=int(args.prefilter), sampling=args.sampling, interp=interp)
+    opts = mk(args.fp16, args.interp)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
-    for _ in range(args.warmup):
-        eng.run(job)
-        eng.synchronize()
-
-    # ---- resident: per-step CUDA-event time on the engine's stream ----
-    step_ms, sweep_ms, hyps = [], [], []
-    launches_per_step = 0
-    barrier(world)
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.random_(0, 255)  # L2 flush, outside the timed events
-            torch.cuda.synchronize()
-            h0 = eng.stats().hypotheses_evaluated
-            eng.run(job)
-            eng.synchronize()
-            st = eng.stats()
-            step_ms.append(st.last_run_ms)
-            sweep_ms.append(st.last_sweep_ms)
-            hyps.append(st.hypotheses_evaluated - h0)
-            launches_per_step = st.last_sweep_launches + 3  # init, refine, output
-    barrier(world)
+    clk = ClockSampler(local)
+    step_ms, sweep_ms, hyps, launches_per_step, dm = time_form(M, views, cfg, opts, args.steps, args.warmup, flush,
+                                                               world, clk)
     total_ms = barrier_max(world, float(sum(step_ms)))
     value = world * args.steps / (total_ms / 1000.0)
+    acc = accuracy(dm, sc.ref.depth)
+
+    plain = None
+    if not args.plain and not args.chosen_only:
+        p_ms, _, _, _, p_dm = time_form(M, views, cfg, mk(False, 0), args.steps, args.warmup, flush, world)
+        p_total = barrier_max(world, float(sum(p_ms)))
+        both = np.isfinite(dm.depth) & np.isfinite(p_dm.depth)
+        d = np.abs(dm.depth[both].astype(np.float64) - p_dm.depth[both]) / p_dm.depth[both]
+        plain = {"value": world * args.steps / (p_total / 1000.0), "unit": "depth maps/s",
+                 "ms_per_step": p_total / args.steps, "storage": "fp32", "interp": "exact fp32",
+                 "accuracy": accuracy(p_dm, sc.ref.depth),
+                 "chosen_vs_plain_median_rel_depth_diff": float(np.median(d)) if d.size else None,
+                 "chosen_vs_plain_p95_rel_depth_diff": float(np.quantile(d, 0.95)) if d.size else None}
 
     # ---- end to end through the C ABI from host buffers ----
-    dm = M.DepthMap.allocate(W, H)
     e2e_times = []
-    for i in range(args.e2e_steps + 1):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        j = eng.stage(views, cfg, undistort=True)
-        eng.run(j)
-        eng.download(j, dm)
-        eng.release(j)
-        t1 = time.perf_counter()
-        if i > 0:
-            e2e_times.append(t1 - t0)
+    if args.e2e_steps > 0:
+        eng = M.Engine(opts)
+        dmh = M.DepthMap.allocate(W, H)
+        for i in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            j = eng.stage(views, cfg, undistort=True)
+            eng.run(j)
+            eng.download(j, dmh)
+            eng.release(j)
+            t1 = time.perf_counter()
+            if i > 0:
+                e2e_times.append(t1 - t0)
+        eng.close()
     e2e_s = barrier_max(world, statistics.mean(e2e_times)) if e2e_times else float("nan")
     e2e_value = world / e2e_s
     h2d = (1 + S_SRC) * W * H
@@ -336,26 +391,18 @@ def run_gpu(args):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("plane_sweep_bytes_per_launch_full")
+            traffic = json.load(f).get("plane_sweep_bytes_per_launch", {}).get(WORKLOAD)
 
-    # accuracy of this map vs analytic truth (reported, not timed)
-    err = np.abs(dm.depth.astype(np.float64) - sc.ref.depth)
-    rel = err / sc.ref.depth
-    ok = np.isfinite(rel)
-    acc = {"filled": float(np.isfinite(dm.depth).mean()),
-           "median_rel_err": float(np.median(rel[ok])) if ok.any() else None,
-           "p95_rel_err": float(np.quantile(rel[ok], 0.95)) if ok.any() else None,
-           "median_abs_err_mm": float(np.median(err[ok]) * 1e3) if ok.any() else None}
-
+    form = "fp16 storage, texture-unit interpolation" if (args.fp16 and args.interp) else \
+        f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} interpolation"
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp16-storage/f32" if args.fp16 else "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 storage)" if args.fp16 else "f32",
             "data": "synthetic (seeded tabletop scene, analytic truth)",
             "config": {"workload": f"{'tabletop' if WORKLOAD == 'c2' else 'sphere'} {W}x{H}, {S_SRC} sources, "
-                                   f"{K}x{K}, {ITERS} iterations, "
-                                   f"plane mode, best_k={args.best_k}, golden-section refine",
-                       "storage": "fp16" if args.fp16 else "fp32", "prefilter": bool(args.prefilter),
-                       "sampling": args.sampling, "interp": "texture-unit" if args.interp else "exact fp32",
+                                   f"{K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}, "
+                                   f"golden-section refine",
+                       "form": form, "prefilter": bool(args.prefilter), "sampling": args.sampling,
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
@@ -369,12 +416,11 @@ def run_gpu(args):
                          "hypotheses_per_launch": hyp_per_launch, "ms_per_launch": per_launch_ms,
                          "flop_per_hypothesis": FLOP_PER_HYP},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
-            "accuracy": acc, "clocks": clk.summary()}
+            "accuracy": acc, "plain_fp32": plain, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline:
         secs, threads, note = cpu_reference_sample(sc)
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
                                 "sample": note}
-    eng.close()
     if rank == 0:
         print(json.dumps(line))
 
@@ -386,15 +432,25 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--best-k", type=int, default=4)
-    ap.add_argument("--fp16", action="store_true")
+    ap.add_argument("--fp16", action="store_true", default=None)
+    ap.add_argument("--plain", action="store_true",
+                    help="time only the plain path: FP32 storage, exact FP32 interpolation")
+    ap.add_argument("--chosen-only", action="store_true", help="skip timing the plain path beside the chosen form")
     ap.add_argument("--prefilter", action="store_true", help="3x3 binomial pre-filter at staging")
     ap.add_argument("--sampling", type=int, default=0, help="0 pixel-centre windows, 1 the reference's convention")
-    ap.add_argument("--interp", type=int, default=0, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
+    ap.add_argument("--interp", type=int, default=None, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "small"])
     args = ap.parse_args()
     set_workload(args.workload)
+    # the chosen form (default): FP16 storage + texture-unit interpolation;
+    # the plain FP32 path is timed beside it unless --plain asks for it alone
+    if args.plain:
+        args.fp16, args.interp = False, 0
+    else:
+        args.fp16 = True if args.fp16 is None else args.fp16
+        args.interp = 1 if args.interp is None else args.interp
     if args.impl == "reference":
         run_reference_arm(args)
     else:
