@@ -105,20 +105,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def make_scene(device):
+def make_scenes(device):
+    """The step's reference views (one MvsScene each)."""
     import synthetic as Syn
 
     if WORKLOAD == "small":
-        return Syn.sphere_on_backdrop(width=W, height=H, f=F, num_sources=S_SRC, seed=1, device=device)
-    return Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device)
+        return [Syn.sphere_on_backdrop(width=W, height=H, f=F, num_sources=S_SRC, seed=1, device=device)]
+    if WORKLOAD == "c3":
+        return Syn.orbit_capture(n_frames=120, n_refs=48, seed=3, device=device)
+    cap = Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device)
+    return [Syn.as_reference(cap, k) for k in range(len(cap.views))]
 
 
 WORKLOAD = "c2"
 
 
 def set_workload(name):
-    """c2: the headline 1920x1440 x 8 sources; small: the 640x480 x 4
-    sources sphere scene (profiling captures, CPU-runnable size)."""
+    """c2: the headline capture -- 9 views at 1920x1440, each the reference
+    of one depth map with the other 8 as its sources; small: the 640x480 x 4
+    sources sphere scene (one map; profiling captures, CPU-runnable size);
+    c3: 48 references from a 120-frame orbit, mixed resolutions, 6-10
+    sources each."""
     global WORKLOAD, W, H, F, ITERS, S_SRC, FLOP_PER_HYP
     WORKLOAD = name
     if name == "small":
@@ -194,6 +201,8 @@ def cpu_reference_sample(sc, cols=480, refine_rows=4, threads=None):
     O.build_oracle(ref=False)
     orc = O.load("oracle")
     threads = threads or os.cpu_count() or 1
+    W, H = sc.ref.camera.width, sc.ref.camera.height
+    cols = min(cols, W)
     rows = min(H, 16 * threads)
     cams = [sc.ref.camera] + [s.camera for s in sc.sources]
     und = [c.undistorted() for c in cams]
@@ -241,7 +250,7 @@ def run_reference_arm(args):
     world, rank, _ = dist_init()
     if rank != 0:
         return
-    sc = make_scene("cpu")
+    sc = make_scenes("cpu")[0]
     secs = []
     threads = os.cpu_count() or 1
     note = ""
@@ -267,16 +276,18 @@ def run_reference_arm(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 
-def time_form(M, views, cfg, opts, steps, warmup, flush, world, sampler=None):
-    """Stage once, run `warmup` untimed steps, then `steps` timed steps (CUDA
-    events on the engine stream; L2 flushed between steps, outside the
-    events).  Returns per-step ms, sweep ms, hypotheses, launches/step, map."""
+def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, sampler=None):
+    """Stage the step's views once, run `warmup` untimed steps, then `steps`
+    timed steps (CUDA events on the engine stream around the whole run; L2
+    flushed between steps, outside the events).  A step runs every view:
+    as one batch, or one launch per view when opts.per_view = 1.  Returns
+    per-step ms, sweep ms, hypotheses, launches/step, maps, stats."""
     import torch
 
     eng = M.Engine(opts)
-    job = eng.stage(views, cfg, undistort=True)
+    jobs = [eng.stage(v, c, undistort=undistort) for v, c in zip(views, cfgs)]
     for _ in range(warmup):
-        eng.run(job)
+        eng.run_many(jobs)
         eng.synchronize()
     step_ms, sweep_ms, hyps = [], [], []
     launches = 0
@@ -287,18 +298,21 @@ def time_form(M, views, cfg, opts, steps, warmup, flush, world, sampler=None):
             flush.random_(0, 255)
             torch.cuda.synchronize()
             h0 = eng.stats().hypotheses_evaluated
-            eng.run(job)
+            eng.run_many(jobs)
             eng.synchronize()
             st = eng.stats()
             step_ms.append(st.last_run_ms)
             sweep_ms.append(st.last_sweep_ms)
             hyps.append(st.hypotheses_evaluated - h0)
-            launches = st.last_sweep_launches + 3  # init, refine, output
     barrier(world)
-    dm = eng.download(job)
-    eng.release(job)
+    st = eng.stats()
+    groups = len(jobs) if opts.per_view else -(-len(jobs) // 64)
+    launches = st.last_sweep_launches + 3 * groups  # + init, refine, output per group
+    maps = [eng.download(j) for j in jobs]
+    for j in jobs:
+        eng.release(j)
     eng.close()
-    return step_ms, sweep_ms, hyps, launches, dm
+    return step_ms, sweep_ms, hyps, launches, maps, st
 
 
 class _Null:
@@ -309,16 +323,35 @@ class _Null:
         return False
 
 
-def accuracy(dm, truth):
+def accuracy(maps, truths):
+    """Pooled over the step's maps: relative depth error vs analytic truth."""
     import numpy as np
 
-    err = np.abs(dm.depth.astype(np.float64) - truth)
-    rel = err / truth
-    ok = np.isfinite(rel)
-    return {"filled": float(np.isfinite(dm.depth).mean()),
-            "median_rel_err": float(np.median(rel[ok])) if ok.any() else None,
-            "p95_rel_err": float(np.quantile(rel[ok], 0.95)) if ok.any() else None,
-            "median_abs_err_mm": float(np.median(err[ok]) * 1e3) if ok.any() else None}
+    rel_all, abs_all, filled = [], [], []
+    for dm, truth in zip(maps, truths):
+        err = np.abs(dm.depth.astype(np.float64) - truth)
+        rel = err / truth
+        ok = np.isfinite(rel)
+        rel_all.append(rel[ok])
+        abs_all.append(err[ok])
+        filled.append(float(np.isfinite(dm.depth).mean()))
+    rel = np.concatenate(rel_all) if rel_all else np.zeros(0)
+    err = np.concatenate(abs_all) if abs_all else np.zeros(0)
+    return {"filled": float(np.mean(filled)),
+            "median_rel_err": float(np.median(rel)) if rel.size else None,
+            "p95_rel_err": float(np.quantile(rel, 0.95)) if rel.size else None,
+            "median_abs_err_mm": float(np.median(err) * 1e3) if err.size else None}
+
+
+def agreement(maps_a, maps_b):
+    import numpy as np
+
+    d = []
+    for a, b in zip(maps_a, maps_b):
+        both = np.isfinite(a.depth) & np.isfinite(b.depth)
+        d.append(np.abs(a.depth[both].astype(np.float64) - b.depth[both]) / b.depth[both])
+    d = np.concatenate(d) if d else np.zeros(0)
+    return (float(np.median(d)) if d.size else None), (float(np.quantile(d, 0.95)) if d.size else None)
 
 
 def run_gpu(args):
@@ -331,78 +364,101 @@ def run_gpu(args):
 
     M.load_library()
     peaks, peak_src = load_peaks()
-    sc = make_scene(f"cuda:{local}")
-    views = views_of(M, sc)
-    cfg = config_of(M, sc)
-    mk = lambda fp16, interp: M.Options(mode=M.MODE_PLANE, best_k=args.best_k,
-                                        storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local, refine=1,
-                                        prefilter=int(args.prefilter), sampling=args.sampling, interp=interp)
-    opts = mk(args.fp16, args.interp)
+    scenes = make_scenes(f"cuda:{local}")
+    views = [views_of(M, sc) for sc in scenes]
+    cfgs = [config_of(M, sc) for sc in scenes]
+    truths = [sc.ref.depth for sc in scenes]
+    undistort = WORKLOAD == "c2"
+    n_maps = len(scenes)
+    pixels = [sc.ref.camera.width * sc.ref.camera.height for sc in scenes]
+    n_src = [len(sc.sources) for sc in scenes]
+    # pixel-weighted sources per map: the FLOP model's S for mixed batches
+    s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
+    flop_per_hyp = s_eff * (K * K * 26 + 30) + 40
+    mk = lambda fp16, interp, per_view: M.Options(
+        mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
+        refine=1, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
+        tile_rows=args.tile_rows)
+    opts = mk(args.fp16, args.interp, args.per_view)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
     clk = ClockSampler(local)
-    step_ms, sweep_ms, hyps, launches_per_step, dm = time_form(M, views, cfg, opts, args.steps, args.warmup, flush,
-                                                               world, clk)
+    step_ms, sweep_ms, hyps, launches_per_step, maps, st = time_form(M, views, cfgs, opts, args.steps, args.warmup,
+                                                                     flush, world, undistort, clk)
     total_ms = barrier_max(world, float(sum(step_ms)))
-    value = world * args.steps / (total_ms / 1000.0)
-    acc = accuracy(dm, sc.ref.depth)
+    value = world * n_maps * args.steps / (total_ms / 1000.0)
+    acc = accuracy(maps, truths)
 
     plain = None
     if not args.plain and not args.chosen_only:
-        p_ms, _, _, _, p_dm = time_form(M, views, cfg, mk(False, 0), args.steps, args.warmup, flush, world)
+        p_fp16 = False if WORKLOAD != "c3" else args.fp16
+        p_interp = 0 if WORKLOAD != "c3" else args.interp
+        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True), args.steps,
+                                                      args.warmup, flush, world, undistort)
         p_total = barrier_max(world, float(sum(p_ms)))
-        both = np.isfinite(dm.depth) & np.isfinite(p_dm.depth)
-        d = np.abs(dm.depth[both].astype(np.float64) - p_dm.depth[both]) / p_dm.depth[both]
-        plain = {"value": world * args.steps / (p_total / 1000.0), "unit": "depth maps/s",
-                 "ms_per_step": p_total / args.steps, "storage": "fp32", "interp": "exact fp32",
-                 "accuracy": accuracy(p_dm, sc.ref.depth),
-                 "chosen_vs_plain_median_rel_depth_diff": float(np.median(d)) if d.size else None,
-                 "chosen_vs_plain_p95_rel_depth_diff": float(np.quantile(d, 0.95)) if d.size else None}
+        med, p95 = agreement(maps, p_maps)
+        plain = {"value": world * n_maps * args.steps / (p_total / 1000.0), "unit": "depth maps/s",
+                 "ms_per_step": p_total / args.steps, "storage": "fp16" if p_fp16 else "fp32",
+                 "interp": "texture-unit" if p_interp else "exact fp32", "launch": "one launch per view",
+                 "gpu_launches_per_step": p_launches, "accuracy": accuracy(p_maps, truths),
+                 "chosen_vs_plain_median_rel_depth_diff": med, "chosen_vs_plain_p95_rel_depth_diff": p95}
 
     # ---- end to end through the C ABI from host buffers ----
     e2e_times = []
     if args.e2e_steps > 0:
         eng = M.Engine(opts)
-        dmh = M.DepthMap.allocate(W, H)
+        dmh = [M.DepthMap.allocate(sc.ref.camera.width, sc.ref.camera.height) for sc in scenes]
         for i in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            j = eng.stage(views, cfg, undistort=True)
-            eng.run(j)
-            eng.download(j, dmh)
-            eng.release(j)
+            jobs = [eng.stage(v, c, undistort=undistort) for v, c in zip(views, cfgs)]
+            eng.run_many(jobs)
+            for j, d in zip(jobs, dmh):
+                eng.download(j, d)
+            for j in jobs:
+                eng.release(j)
             t1 = time.perf_counter()
             if i > 0:
                 e2e_times.append(t1 - t0)
         eng.close()
     e2e_s = barrier_max(world, statistics.mean(e2e_times)) if e2e_times else float("nan")
-    e2e_value = world / e2e_s
-    h2d = (1 + S_SRC) * W * H
-    d2h = W * H * (4 + 1 + 4 + 12 + 4) + 4
+    e2e_value = world * n_maps / e2e_s
+    h2d = int(sum(sc.ref.image.size + sum(s.image.size for s in sc.sources) for sc in scenes))
+    d2h = int(sum(p * (4 + 1 + 4 + 12 + 4) + 4 for p in pixels))
 
     # ---- roofline of the dominant kernel (the red-black sweep) ----
-    sweeps = launches_per_step - 3
-    per_launch_ms = statistics.mean(sweep_ms) / max(1, sweeps)
-    hyp_per_launch = statistics.mean(hyps) / max(1, sweeps)
-    achieved_tflops = FLOP_PER_HYP * hyp_per_launch / (per_launch_ms * 1e-3) / 1e12
+    sweeps = max(1, st.last_sweep_launches)
+    per_launch_ms = statistics.mean(sweep_ms) / sweeps
+    hyp_per_launch = statistics.mean(hyps) / sweeps
+    achieved_tflops = flop_per_hyp * hyp_per_launch / (per_launch_ms * 1e-3) / 1e12
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     peak_tflops = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("plane_sweep_bytes_per_launch", {}).get(WORKLOAD)
+            traffic = json.load(f).get("plane_sweep_bytes_per_launch", {}).get(
+                f"{WORKLOAD}{'_per_view' if args.per_view else ''}")
 
-    form = "fp16 storage, texture-unit interpolation" if (args.fp16 and args.interp) else \
-        f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} interpolation"
+    form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
+            f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}")
+    if WORKLOAD == "c2":
+        wl = (f"tabletop capture: 9 views {W}x{H} (k1=0.05, k2=-0.01, undistorted on the device), each the "
+              f"reference of one map with the other {S_SRC} as sources")
+    elif WORKLOAD == "c3":
+        wl = (f"orbit capture: {n_maps} references from 120 frames, mixed 640x480/1280x960/1920x1440, "
+              f"{min(n_src)}-{max(n_src)} sources")
+    else:
+        wl = f"sphere {W}x{H}, {S_SRC} sources"
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 storage)" if args.fp16 else "f32",
-            "data": "synthetic (seeded tabletop scene, analytic truth)",
-            "config": {"workload": f"{'tabletop' if WORKLOAD == 'c2' else 'sphere'} {W}x{H}, {S_SRC} sources, "
-                                   f"{K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}, "
+            "data": "synthetic (seeded scenes, analytic truth)",
+            "config": {"workload": f"{wl}; {K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}, "
                                    f"golden-section refine",
-                       "form": form, "prefilter": bool(args.prefilter), "sampling": args.sampling,
+                       "maps_per_step": n_maps, "megapixels_per_step": sum(pixels) / 1e6,
+                       "form": form, "tile_rows": st.tile_rows, "ctas_per_sm": st.ctas_per_sm,
+                       "prefilter": bool(args.prefilter), "sampling": args.sampling,
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
@@ -414,11 +470,11 @@ def run_gpu(args):
                          "peak_source": f"{SM_COUNT} SMs x {FP32_LANES} FP32 lanes x 2 x sm_max_mhz {sm_mhz} "
                                         f"({peak_src} MEASURED_PEAKS.json clock)",
                          "hypotheses_per_launch": hyp_per_launch, "ms_per_launch": per_launch_ms,
-                         "flop_per_hypothesis": FLOP_PER_HYP},
+                         "flop_per_hypothesis": flop_per_hyp},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
-            "accuracy": acc, "plain_fp32": plain, "clocks": clk.summary()}
+            "accuracy": acc, "plain": plain, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline:
-        secs, threads, note = cpu_reference_sample(sc)
+        secs, threads, note = cpu_reference_sample(scenes[0])
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
                                 "sample": note}
     if rank == 0:
@@ -428,7 +484,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--best-k", type=int, default=4)
@@ -441,13 +497,15 @@ def main():
     ap.add_argument("--interp", type=int, default=None, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "small"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3"])
+    ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
+    ap.add_argument("--tile-rows", type=int, default=0, help="sweep tile rows (2, 4, 8); 0 = autotuned")
     args = ap.parse_args()
     set_workload(args.workload)
     # the chosen form (default): FP16 storage + texture-unit interpolation;
     # the plain FP32 path is timed beside it unless --plain asks for it alone
     if args.plain:
-        args.fp16, args.interp = False, 0
+        args.fp16, args.interp, args.per_view = False, 0, True
     else:
         args.fp16 = True if args.fp16 is None else args.fp16
         args.interp = 1 if args.interp is None else args.interp

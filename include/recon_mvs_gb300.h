@@ -142,7 +142,12 @@ typedef struct recon_mvs_options {
   int32_t interp;     /* plane mode: 0 = exact FP32 bilinear interpolation (2x2 texel gather);
                          1 = the texture unit's bilinear filter (8-bit fixed-point weights: ~2x
                          fewer instructions per sample, costs within ~1e-3 of the exact ones) */
-  int32_t reserved[4];
+  int32_t tile_rows;  /* plane mode: rows per work tile of the persistent sweep (2, 4 or 8);
+                         0 = chosen by the autotuner (timed once per batch shape, cached) */
+  int32_t per_view;   /* plane mode: 0 = the jobs of one run form one batch -- one launch per
+                         stage over all of them, captured once as a CUDA graph and replayed;
+                         1 = the same kernels launched once per view, no graph */
+  int32_t reserved[2];
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list
@@ -204,7 +209,11 @@ typedef struct recon_mvs_stats {
   double last_run_ms;            /* device time of the last PatchMatch run (CUDA events) */
   double last_sweep_ms;          /* device time of its sweeps only */
   int32_t last_sweep_launches;
-  int32_t reserved[5];
+  int32_t tile_rows;             /* sweep tile rows of the last plane run */
+  int32_t ctas_per_sm;           /* its persistent blocks per SM */
+  int32_t graph_launches;        /* CUDA-graph replays so far */
+  int32_t tune_trials;           /* autotuner searches run by this context */
+  int32_t reserved[1];
 } recon_mvs_stats;
 
 /* ---- version and configuration ---------------------------------------- */
@@ -304,7 +313,9 @@ RECON_API void recon_mvs_context_destroy(void* ctx);
 RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* views, const recon_mvs_config* cfg,
                                            int32_t undistort, int32_t* out_job);
 /* Run PatchMatch (+ refinement per options) on staged jobs, asynchronously
- * on the context's stream. */
+ * on the context's stream.  Plane-mode jobs of one call run as one batch
+ * (options.per_view); running the same job list again replays the batch's
+ * captured CUDA graph.  Results do not depend on the batching. */
 RECON_API recon_status recon_mvs_job_run(void* ctx, int32_t job);
 RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_t n);
 /* Copy a finished job's map to the host (synchronises). */

@@ -189,6 +189,18 @@ struct Job {
   int best_k;
   uint64_t seed;
   unsigned long long* eval_counter;  // optional: hypotheses whose windows were evaluated
+  // plane-mode run parameters (read by the batched kernels per work item)
+  const float* seed_depth;  // optional per-32-px-cell seed depth, seed_gx cells per row
+  int seed_gx;
+  int iterations;           // red-black iterations of this job
+  int refine_iters;         // golden-section steps; 0 = no refinement
+  float inv_per_px;         // refinement half-range: 1 px of disparity in inverse depth
+  float* out_depth;
+  uint8_t* out_support;
+  float* out_conf;
+  float* out_normal;        // optional
+  float* out_cost;          // optional
+  unsigned int* out_filled; // zeroed by the init kernel, counted by the output kernel
 };
 
 // Per-pixel ray of the reference camera, FP64: pinhole fast path, or the

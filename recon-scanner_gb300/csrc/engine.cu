@@ -20,6 +20,7 @@
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "kernels.h"
@@ -208,12 +209,71 @@ struct JobData {
   Job J{};
 };
 
+// ---- plane-mode batch plans (used by the context below) ----
+// Rows per sweep tile the autotuner chooses from (blocks of 32 x rows).
+static const int kRowChoices[] = {2, 4, 8};
+constexpr int kNumRowChoices = 3;
+static int row_choice_index(int rows) {
+  for (int i = 0; i < kNumRowChoices; ++i)
+    if (kRowChoices[i] == rows) return i;
+  return -1;
+}
+
+struct TuneKey {
+  int device, patch_half, hw, storage, max_src, njobs;
+  long long pixels;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, patch_half, hw, storage, max_src, njobs, pixels) <
+           std::tie(o.device, o.patch_half, o.hw, o.storage, o.max_src, o.njobs, o.pixels);
+  }
+};
+struct TuneChoice {
+  int rows = 4;
+  int ctas_per_sm = 0;
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneChoice>& tune_cache() {
+  static std::map<TuneKey, TuneChoice> m;
+  return m;
+}
+
+struct PlaneGroup {
+  std::vector<JobData*> jobs;  // run order: iterations descending, then pixels descending
+  int patch_half = 5;
+  bool hw = false;
+  int max_src = 1, max_iters = 0;
+  bool refine_any = false;
+  long long pixels = 0;
+  std::unique_ptr<PlaneBatch> pix;                    // 32 x 4 pixel tiles
+  std::unique_ptr<PlaneBatch> sweep[kNumRowChoices];  // 64-column x rows sweep tiles
+  std::vector<int> active;  // active[it] = jobs with more than `it` iterations
+  DevArray<int> queues;     // one work counter per half-sweep
+  int rows = 4, ctas_per_sm = 1, grid = 1;
+
+  int nj() const { return (int)jobs.size(); }
+  const PlaneBatch& sweep_batch(int rows_) const { return *sweep[row_choice_index(rows_)]; }
+  int sweep_total(int rows_, int it) const { return sweep_batch(rows_).start[active[it]]; }
+};
+
+struct PlanePlan {
+  std::vector<int> ids;
+  bool per_view = false;
+  std::vector<std::unique_ptr<PlaneGroup>> groups;
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // init, sweeps, refine + output
+  int sweep_launches = 0;
+  ~PlanePlan() {
+    for (auto e : exec)
+      if (e) cudaGraphExecDestroy(e);
+  }
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
   recon_mvs_options opts{};
   std::map<int, std::unique_ptr<JobData>> jobs;
   int next_id = 1;
+  std::unique_ptr<PlanePlan> plan;  // the last batch run, with its captured graph
   DevArray<unsigned long long> counter;
   DevArray<uint8_t> stage_u8;
   DevArray<float> stage_f32;
@@ -228,6 +288,8 @@ struct Context {
   recon_mvs_stats stats{};
 
   explicit Context(const recon_mvs_options& o) : opts(o) {
+    if (o.tile_rows != 0 && row_choice_index(o.tile_rows) < 0)
+      fail(RECON_ERR_INVALID_ARGUMENT, "tile_rows must be 0 (autotuned), 2, 4 or 8");
     device = o.device;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -242,6 +304,7 @@ struct Context {
   ~Context() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    plan.reset();
     jobs.clear();
     for (auto& e : copy_done)
       if (e) cudaEventDestroy(e);
@@ -343,6 +406,24 @@ static const void* upload_image(Context& C, const uint8_t* host, int w, int h, c
     out = f32.p;
   }
   return out;
+}
+
+// Seeds -> per-32-px-cell mean depth (patchmatch_stereo.cpp:499-533).
+static void cell_depths(const JobData& D, std::vector<double>* cell_sum, std::vector<int>* cell_n, int* gx, int* gy) {
+  const int grid = 32;
+  *gx = (D.w + grid - 1) / grid;
+  *gy = (D.h + grid - 1) / grid;
+  cell_sum->assign((size_t)(*gx) * (*gy), 0.0);
+  cell_n->assign((size_t)(*gx) * (*gy), 0);
+  for (size_t i = 0; i + 2 < D.seeds.size(); i += 3) {
+    const double su = D.seeds[i], sv = D.seeds[i + 1], sd = D.seeds[i + 2];
+    if (su < 0 || sv < 0 || su >= D.w || sv >= D.h) continue;
+    if (sd <= 0.0) continue;
+    const int cx = std::min(*gx - 1, (int)su / grid);
+    const int cy = std::min(*gy - 1, (int)sv / grid);
+    (*cell_sum)[(size_t)cy * (*gx) + cx] += sd;
+    (*cell_n)[(size_t)cy * (*gx) + cx] += 1;
+  }
 }
 
 static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,
@@ -508,6 +589,32 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   }
   D.out_cost.alloc(npx);
   D.filled.alloc(1);
+  if (plane) {
+    if (!D.seeds.empty()) {
+      // seeds -> per-32-px-cell mean depth (patchmatch_stereo.cpp:499-533)
+      std::vector<double> sum;
+      std::vector<int> cnt;
+      int gx, gy;
+      cell_depths(D, &sum, &cnt, &gx, &gy);
+      std::vector<float> sd(sum.size(), 0.f);
+      for (size_t i = 0; i < sum.size(); ++i)
+        if (cnt[i] > 0) sd[i] = (float)(sum[i] / (double)cnt[i]);
+      D.seed_depth.alloc(sd.size());
+      CK(cudaMemcpyAsync(D.seed_depth.p, sd.data(), sd.size() * sizeof(float), cudaMemcpyHostToDevice, C.stream));
+      D.seed_gx = gx;
+      J.seed_depth = D.seed_depth.p;
+      J.seed_gx = gx;
+    }
+    J.iterations = cfg->iterations;
+    J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0) ? cfg->subpixel_iterations : 0;
+    J.inv_per_px = (float)D.inv_per_px;
+    J.out_depth = D.out_depth.p;
+    J.out_support = D.out_support.p;
+    J.out_conf = D.out_conf.p;
+    J.out_normal = D.out_normal.p;
+    J.out_cost = D.out_cost.p;
+    J.out_filled = D.filled.p;
+  }
   CK(cudaStreamSynchronize(C.stream));
   const int id = C.next_id++;
   C.jobs[id] = std::move(jd);
@@ -520,58 +627,235 @@ static JobData& get_job(Context& C, int id) {
   return *it->second;
 }
 
-// Seeds -> per-32-px-cell mean depth (patchmatch_stereo.cpp:499-533).
-static void cell_depths(const JobData& D, std::vector<double>* cell_sum, std::vector<int>* cell_n, int* gx, int* gy) {
-  const int grid = 32;
-  *gx = (D.w + grid - 1) / grid;
-  *gy = (D.h + grid - 1) / grid;
-  cell_sum->assign((size_t)(*gx) * (*gy), 0.0);
-  cell_n->assign((size_t)(*gx) * (*gy), 0);
-  for (size_t i = 0; i + 2 < D.seeds.size(); i += 3) {
-    const double su = D.seeds[i], sv = D.seeds[i + 1], sd = D.seeds[i + 2];
-    if (su < 0 || sv < 0 || su >= D.w || sv >= D.h) continue;
-    if (sd <= 0.0) continue;
-    const int cx = std::min(*gx - 1, (int)su / grid);
-    const int cy = std::min(*gy - 1, (int)sv / grid);
-    (*cell_sum)[(size_t)cy * (*gx) + cx] += sd;
-    (*cell_n)[(size_t)cy * (*gx) + cx] += 1;
+// ---- plane mode -----------------------------------------------------------
+// Plane-mode jobs run in batches: the jobs of one recon_mvs_jobs_run call that
+// share the window size and interpolation mode form a group, and each stage
+// (init, every half-sweep, refinement, output) is ONE launch over the whole
+// group -- the half-sweeps a persistent kernel pulling tiles of all the
+// group's views from a work counter.  The run is captured once as a CUDA
+// graph and replayed while the same jobs are run again.  The per-view form
+// (options.per_view = 1) launches the same kernels once per view instead,
+// without a graph: the comparison the batched form is measured against.
+
+static void build_group(Context& C, PlaneGroup& G) {
+  std::stable_sort(G.jobs.begin(), G.jobs.end(), [](const JobData* a, const JobData* b) {
+    if (a->cfg.iterations != b->cfg.iterations) return a->cfg.iterations > b->cfg.iterations;
+    return (long long)a->w * a->h > (long long)b->w * b->h;
+  });
+  const int n = G.nj();
+  if (n < 1 || n > kBatchJobs) fail(RECON_ERR_INTERNAL, "batch group size out of range");
+  G.pix = std::make_unique<PlaneBatch>();
+  std::memset(G.pix.get(), 0, sizeof(PlaneBatch));
+  for (auto& b : G.sweep) {
+    b = std::make_unique<PlaneBatch>();
+    std::memset(b.get(), 0, sizeof(PlaneBatch));
+  }
+  G.max_src = 1;
+  G.max_iters = 0;
+  G.refine_any = false;
+  G.pixels = 0;
+  for (int j = 0; j < n; ++j) {
+    const JobData& D = *G.jobs[j];
+    G.max_src = std::max(G.max_src, D.num_src);
+    G.max_iters = std::max(G.max_iters, std::max(0, D.cfg.iterations));
+    G.refine_any = G.refine_any || D.J.refine_iters > 0;
+    G.pixels += (long long)D.w * D.h;
+    auto add = [&](PlaneBatch& B, long long tiles) {
+      B.jobs[j] = D.J;
+      const long long next = (long long)B.start[j] + tiles;
+      if (next > 0x7fffffffLL) fail(RECON_ERR_INVALID_ARGUMENT, "batch too large: more than 2^31 tiles");
+      B.start[j + 1] = (int)next;
+      B.njobs = n;
+    };
+    add(*G.pix, (long long)((D.w + 31) / 32) * ((D.h + 3) / 4));
+    for (int r = 0; r < kNumRowChoices; ++r)
+      add(*G.sweep[r], (long long)((D.w + 63) / 64) * ((D.h + kRowChoices[r] - 1) / kRowChoices[r]));
+  }
+  G.active.assign(std::max(G.max_iters, 1), 0);
+  for (int it = 0; it < G.max_iters; ++it)
+    for (int j = 0; j < n; ++j)
+      if (G.jobs[j]->cfg.iterations > it) G.active[it] = j + 1;
+  G.queues.alloc(std::max(2 * G.max_iters, 1));
+}
+
+static int sm_count(int device) {
+  int n = 0;
+  CK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device));
+  return std::max(n, 1);
+}
+
+// The autotuner: times one half-sweep of the group itself for every tile
+// shape (rows per tile) and every persistent grid (resident blocks per SM,
+// full or one less), starting each trial from a fresh init, and keeps the
+// fastest.  The choice cannot change results -- every pixel computes the same
+// thing whatever the tile -- and is cached per (device, window, interpolation,
+// storage, max sources, job count, pixel count).  Explicit options.tile_rows
+// skips the search.
+static void tune_group(Context& C, PlaneGroup& G) {
+  const int nsm = sm_count(C.device);
+  auto set_shape = [&](int rows, int ctas) {
+    G.rows = rows;
+    G.ctas_per_sm = ctas;
+    G.grid = ctas * nsm;
+  };
+  auto occupancy = [&](int rows) {
+    int b = 0;
+    CK(plane_sweep_occupancy(G.patch_half, G.hw, G.max_src, rows, &b));
+    return b;
+  };
+  if (C.opts.tile_rows != 0) {
+    const int b = occupancy(C.opts.tile_rows);
+    if (b < 1) fail(RECON_ERR_INVALID_ARGUMENT, "tile_rows: the sweep kernel does not fit on an SM");
+    set_shape(C.opts.tile_rows, b);
+    return;
+  }
+  const TuneKey key{C.device, G.patch_half, G.hw ? 1 : 0, C.opts.storage, G.max_src, G.nj(), G.pixels};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = tune_cache().find(key);
+    if (it != tune_cache().end()) {
+      set_shape(it->second.rows, it->second.ctas_per_sm);
+      return;
+    }
+  }
+  if (G.max_iters == 0) {
+    set_shape(4, std::max(1, occupancy(4)));
+    return;
+  }
+  unsigned long long saved = 0;
+  CK(cudaMemcpyAsync(&saved, C.counter.p, sizeof(saved), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  float best_ms = 1e30f;
+  TuneChoice best;
+  for (int rows : kRowChoices) {
+    const int b = occupancy(rows);
+    for (int ctas = b; ctas >= std::max(1, b - 1); --ctas) {
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {  // the first trial also loads the kernel
+        CK(launch_plane_init(*G.pix, G.patch_half, G.hw, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+        CK(cudaEventRecord(C.ev_sweep0, C.stream));
+        CK(launch_plane_sweep(G.sweep_batch(rows), G.sweep_total(rows, 0), G.queues.p, G.patch_half, G.hw, G.max_src,
+                              rows, ctas * nsm, 0, 0, C.stream));
+        CK(cudaEventRecord(C.ev_sweep1, C.stream));
+        CK(cudaEventSynchronize(C.ev_sweep1));
+        CK(cudaEventElapsedTime(&ms, C.ev_sweep0, C.ev_sweep1));
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.rows = rows;
+        best.ctas_per_sm = ctas;
+      }
+    }
+  }
+  CK(cudaMemcpyAsync(C.counter.p, &saved, sizeof(saved), cudaMemcpyHostToDevice, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache()[key] = best;
+  }
+  set_shape(best.rows, best.ctas_per_sm);
+  C.stats.tune_trials += 1;
+}
+
+// The run of a plan in three stages -- every group's init; the sweeps;
+// every group's refinement and output -- each captured as its own CUDA graph
+// in the batched form, so that the context's timing events sit on the stream
+// between the graph launches and bracket the sweeps exactly.
+static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
+  if (stage == 0) {
+    for (auto& g : P.groups) {
+      PlaneGroup& G = *g;
+      CK(launch_plane_init(*G.pix, G.patch_half, G.hw, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+    }
+  } else if (stage == 1) {
+    int launches = 0;
+    for (auto& g : P.groups) {
+      PlaneGroup& G = *g;
+      for (int it = 0; it < G.max_iters; ++it)
+        for (int color = 0; color < 2; ++color) {
+          CK(launch_plane_sweep(G.sweep_batch(G.rows), G.sweep_total(G.rows, it), G.queues.p + 2 * it + color,
+                                G.patch_half, G.hw, G.max_src, G.rows, G.grid, color, it, C.stream));
+          ++launches;
+        }
+    }
+    P.sweep_launches = launches;
+  } else {
+    for (auto& g : P.groups) {
+      PlaneGroup& G = *g;
+      if (G.refine_any) CK(launch_plane_refine(*G.pix, G.patch_half, G.hw, G.max_src, C.stream));
+      CK(launch_plane_output(*G.pix, C.stream));
+    }
   }
 }
 
-// ---- plane mode -----------------------------------------------------------
-static void run_plane(Context& C, JobData& D) {
-  Job& J = D.J;
-  const float* seed_ptr = nullptr;
-  if (!D.seeds.empty()) {
-    std::vector<double> sum;
-    std::vector<int> cnt;
-    int gx, gy;
-    cell_depths(D, &sum, &cnt, &gx, &gy);
-    std::vector<float> sd(sum.size(), 0.f);
-    for (size_t i = 0; i < sum.size(); ++i)
-      if (cnt[i] > 0) sd[i] = (float)(sum[i] / (double)cnt[i]);
-    D.seed_depth.alloc(sd.size());
-    CK(cudaMemcpyAsync(D.seed_depth.p, sd.data(), sd.size() * sizeof(float), cudaMemcpyHostToDevice, C.stream));
-    D.seed_gx = gx;
-    seed_ptr = D.seed_depth.p;
+static void capture_stage(Context& C, PlanePlan& P, int stage) {
+  CK(cudaStreamBeginCapture(C.stream, cudaStreamCaptureModeThreadLocal));
+  cudaGraph_t graph = nullptr;
+  try {
+    enqueue_stage(C, P, stage);
+  } catch (...) {
+    cudaStreamEndCapture(C.stream, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    throw;
   }
-  CK(cudaEventRecord(C.ev_start, C.stream));
-  CK(launch_plane_init(J, seed_ptr, 32, D.seed_gx, C.stream));
-  CK(cudaEventRecord(C.ev_sweep0, C.stream));
-  int launches = 0;
-  for (int it = 0; it < D.cfg.iterations; ++it) {
-    CK(launch_plane_sweep(J, 0, it, D.cfg.iterations, C.stream));
-    CK(launch_plane_sweep(J, 1, it, D.cfg.iterations, C.stream));
-    launches += 2;
+  CK(cudaStreamEndCapture(C.stream, &graph));
+  const cudaError_t e = cudaGraphInstantiate(&P.exec[stage], graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+}
+
+static void launch_plan(Context& C, PlanePlan& P) {
+  const cudaEvent_t marks[4] = {C.ev_start, C.ev_sweep0, C.ev_sweep1, C.ev_end};
+  CK(cudaEventRecord(marks[0], C.stream));
+  for (int stage = 0; stage < 3; ++stage) {
+    if (P.exec[stage])
+      CK(cudaGraphLaunch(P.exec[stage], C.stream));
+    else
+      enqueue_stage(C, P, stage);
+    CK(cudaEventRecord(marks[stage + 1], C.stream));
   }
-  CK(cudaEventRecord(C.ev_sweep1, C.stream));
-  if (D.opts.refine && D.cfg.subpixel_iterations > 0)
-    CK(launch_plane_refine(J, D.inv_per_px, D.cfg.subpixel_iterations, C.stream));
-  CK(cudaMemsetAsync(D.filled.p, 0, sizeof(unsigned int), C.stream));
-  CK(launch_plane_output(J, D.out_depth.p, D.out_support.p, D.out_conf.p, D.out_normal.p, D.out_cost.p, D.filled.p,
-                         C.stream));
-  CK(cudaEventRecord(C.ev_end, C.stream));
-  C.stats.last_sweep_launches = launches;
+}
+
+static std::unique_ptr<PlanePlan> make_plan(Context& C, const std::vector<JobData*>& jobs,
+                                            const std::vector<int>& ids) {
+  auto P = std::make_unique<PlanePlan>();
+  P->ids = ids;
+  P->per_view = C.opts.per_view != 0;
+  for (JobData* D : jobs) {
+    PlaneGroup* G = nullptr;
+    if (!P->per_view)
+      for (auto& g : P->groups)
+        if (g->patch_half == D->J.patch_half && g->hw == (D->J.hw_interp != 0) && g->nj() < kBatchJobs) G = g.get();
+    if (!G) {
+      P->groups.push_back(std::make_unique<PlaneGroup>());
+      G = P->groups.back().get();
+      G->patch_half = D->J.patch_half;
+      G->hw = D->J.hw_interp != 0;
+    }
+    G->jobs.push_back(D);
+  }
+  for (auto& g : P->groups) build_group(C, *g);
+  for (auto& g : P->groups) tune_group(C, *g);
+  if (!P->per_view)
+    for (int stage = 0; stage < 3; ++stage) capture_stage(C, *P, stage);
+  else
+    P->sweep_launches = 0;
+  return P;
+}
+
+static void run_plane_jobs(Context& C, const std::vector<JobData*>& jobs, const std::vector<int>& ids) {
+  if (jobs.empty()) return;
+  if (!C.plan || C.plan->ids != ids || C.plan->per_view != (C.opts.per_view != 0)) {
+    C.plan.reset();
+    C.plan = make_plan(C, jobs, ids);
+  }
+  PlanePlan& P = *C.plan;
+  launch_plan(C, P);
+  if (P.exec[0]) C.stats.graph_launches += 1;
+  C.stats.last_sweep_launches = P.sweep_launches;
+  C.stats.tile_rows = P.groups[0]->rows;
+  C.stats.ctas_per_sm = P.groups[0]->ctas_per_sm;
 }
 
 // ---- compat mode ----------------------------------------------------------
@@ -692,17 +976,37 @@ static void run_compat(Context& C, JobData& D) {
   C.stats.last_sweep_launches = sweep;
 }
 
-static void run_job(Context& C, JobData& D) {
+// Runs jobs in the given order: plane-mode jobs as one batch, compat-mode
+// jobs (the reference's own sweep order) one after another.
+static void run_jobs(Context& C, const std::vector<int>& ids) {
   C.use();
-  if (D.degenerate) {
-    D.ran = true;
-    return;
+  std::vector<JobData*> plane;
+  std::vector<int> plane_ids;
+  for (int id : ids) {
+    JobData& D = get_job(C, id);
+    if (D.degenerate) continue;
+    if (D.opts.mode == RECON_MVS_MODE_PLANE) {
+      if (std::find(plane_ids.begin(), plane_ids.end(), id) != plane_ids.end())
+        fail(RECON_ERR_INVALID_ARGUMENT, "a job is listed twice");
+      plane.push_back(&D);
+      plane_ids.push_back(id);
+    } else {
+      run_compat(C, D);
+    }
   }
-  if (D.opts.mode == RECON_MVS_MODE_PLANE)
-    run_plane(C, D);
-  else
-    run_compat(C, D);
-  D.ran = true;
+  run_plane_jobs(C, plane, plane_ids);
+  for (int id : ids) get_job(C, id).ran = true;
+}
+
+static void run_job(Context& C, int id) { run_jobs(C, std::vector<int>{id}); }
+
+// Drops a job, and the cached plan when it runs that job.
+static void erase_job(Context& C, int id) {
+  if (C.plan && std::find(C.plan->ids.begin(), C.plan->ids.end(), id) != C.plan->ids.end()) {
+    cudaStreamSynchronize(C.stream);
+    C.plan.reset();
+  }
+  C.jobs.erase(id);
 }
 
 static void finish_stats(Context& C) {
@@ -768,7 +1072,7 @@ static Context& default_context(const recon_mvs_options* opts) {
 struct JobScope {
   Context& C;
   int id;
-  ~JobScope() { C.jobs.erase(id); }
+  ~JobScope() { erase_job(C, id); }
 };
 
 // ---------------------------------------------------------------------------
@@ -1039,9 +1343,8 @@ RECON_API recon_status recon_mvs_patchmatch(const recon_mvs_views* views, const 
     Context& C = default_context(opts);
     const int id = stage_job(C, views, cfg, false, seed_points, num_seeds);
     JobScope scope{C, id};
-    JobData& D = get_job(C, id);
-    run_job(C, D);
-    download_job(C, D, out, out_filled);
+    run_job(C, id);
+    download_job(C, get_job(C, id), out, out_filled);
   });
 }
 
@@ -1349,7 +1652,7 @@ RECON_API recon_status recon_mvs_job_run(void* ctx, int32_t job) {
   return guard([&] {
     if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
     Context& C = *static_cast<Context*>(ctx);
-    run_job(C, get_job(C, job));
+    run_job(C, job);
   });
 }
 
@@ -1357,7 +1660,7 @@ RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_
   return guard([&] {
     if (!ctx || (!jobs && n > 0)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
     Context& C = *static_cast<Context*>(ctx);
-    for (int i = 0; i < n; ++i) run_job(C, get_job(C, jobs[i]));
+    run_jobs(C, std::vector<int>(jobs, jobs + n));
   });
 }
 
@@ -1376,7 +1679,8 @@ RECON_API recon_status recon_mvs_job_release(void* ctx, int32_t job) {
     Context& C = *static_cast<Context*>(ctx);
     C.use();
     CK(cudaStreamSynchronize(C.stream));
-    if (!C.jobs.erase(job)) fail(RECON_ERR_INVALID_ARGUMENT, "unknown job id");
+    get_job(C, job);
+    erase_job(C, job);
   });
 }
 

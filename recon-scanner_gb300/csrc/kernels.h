@@ -52,11 +52,28 @@ struct NccWindow {
 // ---- PatchMatch ----
 cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const int* py, const double* inv,
                              const float* normals, float* cost, int* support, float* view_cost, cudaStream_t st);
-cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st);
-cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters, cudaStream_t st);
-cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st);
-cudaError_t launch_plane_output(const Job& J, float* depth, uint8_t* support, float* conf, float* normal, float* cost,
-                                unsigned int* filled, cudaStream_t st);
+// Plane-mode batches.  A batch's work items are tiles of its jobs, listed
+// job after job; start[j] is the first item of job j and start[njobs] the
+// batch's item count.  Pixel-tile kernels (init, refine, output) use 32 x 4
+// pixel tiles; sweeps use 64-column x rows tiles with their own prefix.  The
+// whole record is a kernel parameter (<= 32 KB): the jobs sit in the
+// constant bank.
+constexpr int kMaxTileRows = 8;
+constexpr int kBatchJobs = 64;
+struct PlaneBatch {
+  Job jobs[kBatchJobs];
+  int start[kBatchJobs + 1];
+  int njobs;
+};
+static_assert(sizeof(PlaneBatch) + 64 <= 32764, "PlaneBatch exceeds the kernel-parameter limit");
+cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, bool hw, int max_src, int* queues, int num_queues,
+                              cudaStream_t st);
+cudaError_t plane_sweep_occupancy(int patch_half, bool hw, int max_src, int rows, int* blocks_per_sm);
+cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, bool hw, int max_src,
+                               int rows, int grid, int color, int iter, cudaStream_t st);
+cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, bool hw, int max_src, cudaStream_t st);
+cudaError_t launch_plane_output(const PlaneBatch& B, cudaStream_t st);
+
 cudaError_t launch_compat_init(const Job& J, float* cost, cudaStream_t st);
 cudaError_t launch_compat_sweep(const Job& J, const double* inv_in, const float* cost_in, const int32_t* sup_in,
                                 double* inv_out, float* cost_out, int32_t* sup_out, const uint32_t* draws,

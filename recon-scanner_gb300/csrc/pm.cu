@@ -229,25 +229,69 @@ __device__ __forceinline__ Rng pixel_rng(const Job& J, int idx, int iter, int sa
   return g;
 }
 
+// ---------------------------------------------------------------------------
+// batched plane kernels
+// ---------------------------------------------------------------------------
+// Every plane-mode run goes through these kernels.  A batch is any set of up
+// to kBatchJobs reference views -- uneven sizes and source counts -- that
+// share the window size and the interpolation mode.  The batch's job records
+// travel in the kernel-parameter (constant) bank: a block reads the record of
+// its job with uniform constant loads, which the compiler can re-issue instead
+// of holding every field in registers (a copy in shared memory costs the
+// unrolled window code hundreds of bytes of spills).  Work items are tiles;
+// B.start holds the exclusive prefix of the jobs' tile counts, so an item
+// finds its job by a binary search.
+__device__ __forceinline__ int find_job(const PlaneBatch& B, int item) {
+  int lo = 0, hi = B.njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (B.start[mid] <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Pixel-tile kernels (init, refine, output): one 32 x 4 block per 32 x 4
+// pixel tile, grid = the batch's tile count.  Returns the block's job and
+// whether this thread's pixel lies inside its image.
+__device__ __forceinline__ bool pixel_item(const PlaneBatch& B, int* job, int* x, int* y) {
+  const int j = find_job(B, (int)blockIdx.x);
+  const int local = (int)blockIdx.x - B.start[j];
+  const int tx = (B.jobs[j].w + 31) >> 5;
+  *job = j;
+  *x = (local % tx) * 32 + (int)threadIdx.x;
+  *y = (local / tx) * 4 + (int)threadIdx.y;
+  return *x < B.jobs[j].w && *y < B.jobs[j].h;
+}
+
+// Random initialisation (and seed cells) + initial cost.  Block 0 also zeroes
+// the work counters of the persistent sweeps that follow, and each job's
+// first pixel zeroes its filled counter.
 template <int H, bool kHw>
-__global__ void __launch_bounds__(128, 4) k_plane_init(Job J, const float* __restrict__ seed_depth, int seed_grid, int seed_gx) {
+__global__ void __launch_bounds__(128, 4) k_plane_init(const __grid_constant__ PlaneBatch B, int* queues,
+                                                       int num_queues) {
   extern __shared__ float2 smem[];
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
-  if (x >= J.w || y >= J.h) return;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  if (blockIdx.x == 0)
+    for (int q = tid; q < num_queues; q += 128) queues[q] = 0;
+  int j, x, y;
+  if (!pixel_item(B, &j, &x, &y)) return;
+  const Job& J = B.jobs[j];
+  PCache pc{smem, 128, tid};
   const int idx = y * J.w + x;
+  if (idx == 0) *J.out_filled = 0u;
   float rx, ry;
   fill_pcache(J, pc, x, y, &rx, &ry);
   Rng g = pixel_rng(J, idx, -1, 1);
   float rho = J.rho_min + (J.rho_max - J.rho_min) * g.uniform();
   float nx, ny, nz;
   random_normal(g, rx, ry, &nx, &ny, &nz);
-  if (seed_depth) {
-    const int cx = min(x / seed_grid, seed_gx - 1);
-    const int cy = y / seed_grid;
-    const float sd = seed_depth[cy * seed_gx + cx];
+  if (J.seed_depth) {
+    const int cx = min(x / 32, J.seed_gx - 1);
+    const int cy = y / 32;
+    const float sd = J.seed_depth[cy * J.seed_gx + cx];
     if (sd > 0.f) {
       rho = 1.0f / sd;
       nx = 0.f;
@@ -310,50 +354,14 @@ __device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t,
   return rw;
 }
 
-// One red-black half-sweep.  A block of 32 x 4 threads owns the 32
-// same-colour pixels of each of 4 rows (64 columns); the reference rows it
-// reads (4 + 2H rows, the 64 columns +- 16) are staged once into shared
-// memory as even / odd column planes from the de-interleaved reference copy.
-template <int H, bool kHw>
-__global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int iter, int num_iters) {
-  extern __shared__ float2 smem[];
-  constexpr int kRows = 4 + 2 * (H > 0 ? H : 1);
-  __shared__ float tile[2][kRows][kTileCols];
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int parity = (y + color) & 1;
-  const int x = blockIdx.x * (2 * blockDim.x) + 2 * threadIdx.x + parity;
-  if constexpr (H > 0) {
-    const int i0 = blockIdx.x * 32 - 8;
-    const int r0 = blockIdx.y * 4 - H;
-    for (int e = tid; e < 2 * kRows * kTileCols; e += 128) {
-      const int p = e / (kRows * kTileCols);
-      const int rr = (e / kTileCols) % kRows;
-      const int j = e % kTileCols;
-      const int row = r0 + rr, col = i0 + j;
-      float v = 0.f;
-      if (row >= 0 && row < J.h && col >= 0 && col < J.ref_half_w) v = J.ref_de[((size_t)p * J.h + row) * J.ref_half_w + col];
-      tile[p][rr][j] = v;
-    }
-    __syncthreads();
-  }
-  if (x >= J.w || y >= J.h) return;
+// One red-black half-sweep of one pixel: propagation from the best-cost
+// neighbour of each of the 8 adaptive regions, then 5 refinement hypotheses.
+template <int H, bool kHw, class RefT>
+__device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, const RefT& ref, const RefWindow& rw,
+                                            int x, int y, int color, int iter) {
   const int idx = y * J.w + x;
   float rx, ry;
   fill_pcache(J, pc, x, y, &rx, &ry);
-  using RefT = std::conditional_t<(H > 0), TileRef, GlobalRef>;
-  RefT ref;
-  if constexpr (H > 0)
-    ref = TileRef{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
-                  (int)threadIdx.x, parity, (int)threadIdx.y};
-  else
-    ref = GlobalRef{J.pref, J.w, x, y};
-  RefWindow rw;
-  if constexpr (H > 0)
-    rw = tile_window<H>(J, ref, x, y);
-  else
-    rw = ref_window(J, x, y, J.half_pixel);
   float4 cur = J.hyp[idx];
   float cur_cost = J.cost[idx];
   int cur_sup = J.support[idx];
@@ -439,11 +447,75 @@ __global__ void __launch_bounds__(128, 5) k_plane_sweep(Job J, int color, int it
   J.support[idx] = (uint8_t)min(cur_sup, 255);
 }
 
-__global__ void k_plane_output(Job J, float* depth, uint8_t* support, float* conf, float* normal, float* cost_out,
-                               unsigned int* filled) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= J.w || y >= J.h) return;
+// One red-black half-sweep over a whole batch: a persistent kernel (grid =
+// resident blocks) whose blocks pull work items -- 64-column x R-row tiles,
+// R = blockDim.y -- from an atomic counter until the batch is exhausted.  A
+// block of 32 x R threads owns the 32 same-colour pixels of each of its R
+// rows; the reference rows the tile reads (R + 2H rows, the 64 columns +- 16)
+// are staged once into shared memory as even / odd column planes from the
+// de-interleaved reference copy.  `queue` is this launch's work counter
+// (zeroed by the init kernel); `total` its item count -- jobs with fewer
+// iterations than `iter + 1` sit at the end of the job order and fall
+// outside it.
+template <int H, bool kHw>
+__global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch B, int total, int* queue, int color,
+                                              int iter) {
+  extern __shared__ float2 smem[];
+  constexpr int kHalo = H > 0 ? H : 1;
+  __shared__ float tile[2][kMaxTileRows + 2 * kHalo][kTileCols];
+  __shared__ int s_item;
+  const int R = (int)blockDim.y;
+  const int nthreads = 32 * R;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const PCache pc{smem, nthreads, tid};
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) break;
+    const int j = find_job(B, item);
+    const Job& J = B.jobs[j];
+    const int local = item - B.start[j];
+    const int tiles_x = (J.w + 63) >> 6;
+    const int bx = local % tiles_x, by = local / tiles_x;
+    const int y = by * R + (int)threadIdx.y;
+    const int parity = (y + color) & 1;
+    const int x = bx * 64 + 2 * (int)threadIdx.x + parity;
+    if constexpr (H > 0) {
+      const int i0 = bx * 32 - 8, r0 = by * R - H;
+      for (int p = 0; p < 2; ++p)
+        for (int rr = threadIdx.y; rr < R + 2 * H; rr += R) {
+          const int row = r0 + rr;
+          const bool row_ok = row >= 0 && row < J.h;
+          const float* src = J.ref_de + ((size_t)p * J.h + (row_ok ? row : 0)) * J.ref_half_w;
+          for (int c = threadIdx.x; c < kTileCols; c += 32) {
+            const int col = i0 + c;
+            tile[p][rr][c] = (row_ok && col >= 0 && col < J.ref_half_w) ? src[col] : 0.f;
+          }
+        }
+      __syncthreads();
+    }
+    if (x < J.w && y < J.h) {
+      if constexpr (H > 0) {
+        const TileRef ref{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
+                          (int)threadIdx.x, parity, (int)threadIdx.y};
+        const RefWindow rw = tile_window<H>(J, ref, x, y);
+        sweep_pixel<H, kHw>(J, pc, ref, rw, x, y, color, iter);
+      } else {
+        const GlobalRef ref{J.pref, J.w, x, y};
+        const RefWindow rw = ref_window(J, x, y, J.half_pixel);
+        sweep_pixel<H, kHw>(J, pc, ref, rw, x, y, color, iter);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Final maps of every job of the batch.
+__global__ void __launch_bounds__(128) k_plane_output(const __grid_constant__ PlaneBatch B) {
+  int j, x, y;
+  if (!pixel_item(B, &j, &x, &y)) return;
+  const Job& J = B.jobs[j];
   const int idx = y * J.w + x;
   const float4 h = J.hyp[idx];
   const float c = J.cost[idx];
@@ -456,18 +528,18 @@ __global__ void k_plane_output(Job J, float* depth, uint8_t* support, float* con
       d = dd;
       cf = 1.0f - fminf(1.0f, fmaxf(0.0f, c));
       sp = J.support[idx];
-      atomicAdd(filled, 1u);
+      atomicAdd(J.out_filled, 1u);
     }
   }
-  depth[idx] = d;
-  support[idx] = sp;
-  conf[idx] = cf;
-  if (normal) {
-    normal[3 * idx] = h.y;
-    normal[3 * idx + 1] = h.z;
-    normal[3 * idx + 2] = h.w;
+  J.out_depth[idx] = d;
+  J.out_support[idx] = sp;
+  J.out_conf[idx] = cf;
+  if (J.out_normal) {
+    J.out_normal[3 * idx] = h.y;
+    J.out_normal[3 * idx + 1] = h.z;
+    J.out_normal[3 * idx + 2] = h.w;
   }
-  if (cost_out) cost_out[idx] = c;
+  if (J.out_cost) J.out_cost[idx] = c;
 }
 
 // ---------------------------------------------------------------------------
@@ -739,13 +811,14 @@ __global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per
 // the pixel's own plane normal over +-1 px of disparity, the reference's
 // refinement schedule applied to the plane cost.
 template <int H, bool kHw>
-__global__ void __launch_bounds__(128, 4) k_plane_refine(Job J, double inv_per_px, int subpixel_iterations) {
+__global__ void __launch_bounds__(128, 4) k_plane_refine(const __grid_constant__ PlaneBatch B) {
   extern __shared__ float2 smem[];
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  PCache pc{smem, (int)(blockDim.x * blockDim.y), tid};
-  if (x >= J.w || y >= J.h) return;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  int j, x, y;
+  if (!pixel_item(B, &j, &x, &y)) return;
+  const Job& J = B.jobs[j];
+  if (J.refine_iters <= 0) return;
+  PCache pc{smem, 128, tid};
   const int idx = y * J.w + x;
   const float4 h0 = J.hyp[idx];
   const float c0 = J.cost[idx];
@@ -759,13 +832,13 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine(Job J, double inv_per_p
   };
   float best_d = h0.x, best_c = c0;
   int best_s = J.support[idx];
-  float lo = fmaxf(J.rho_min, best_d - (float)inv_per_px);
-  float hi = fminf(J.rho_max, best_d + (float)inv_per_px);
+  float lo = fmaxf(J.rho_min, best_d - J.inv_per_px);
+  float hi = fminf(J.rho_max, best_d + J.inv_per_px);
   if (hi > lo) {
     const float inv_phi = 0.618033988749895f;
     float c1 = hi - inv_phi * (hi - lo), c2 = lo + inv_phi * (hi - lo);
     HypCost f1 = eval(c1), f2 = eval(c2);
-    for (int k = 0; k < subpixel_iterations; ++k) {
+    for (int k = 0; k < J.refine_iters; ++k) {
       if (f1.cost < f2.cost) {
         hi = c2;
         c2 = c1;
@@ -963,74 +1036,82 @@ cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const
 
 static dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
 
-cudaError_t launch_plane_init(const Job& J, const float* seed_depth, int seed_grid, int seed_gx, cudaStream_t st) {
-  const dim3 b(32, 4);
-  const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.hw_interp) {
-    if (J.patch_half == 5)
-      k_plane_init<5, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-    else if (J.patch_half == 3)
-      k_plane_init<3, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-    else
-      k_plane_init<0, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-  } else {
-    if (J.patch_half == 5)
-      k_plane_init<5, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-    else if (J.patch_half == 3)
-      k_plane_init<3, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
-    else
-      k_plane_init<0, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, seed_depth, seed_grid, seed_gx);
+// Calls f(integral_constant<H>, bool_constant<kHw>) for the compiled window
+// sizes (11x11, 7x7, and the generic runtime-size path).
+template <class F>
+static cudaError_t dispatch_plane(int patch_half, bool hw, F&& f) {
+  if (hw) {
+    if (patch_half == 5) return f(std::integral_constant<int, 5>{}, std::true_type{});
+    if (patch_half == 3) return f(std::integral_constant<int, 3>{}, std::true_type{});
+    return f(std::integral_constant<int, 0>{}, std::true_type{});
   }
-  return cudaGetLastError();
+  if (patch_half == 5) return f(std::integral_constant<int, 5>{}, std::false_type{});
+  if (patch_half == 3) return f(std::integral_constant<int, 3>{}, std::false_type{});
+  return f(std::integral_constant<int, 0>{}, std::false_type{});
 }
 
-cudaError_t launch_plane_sweep(const Job& J, int color, int iter, int num_iters, cudaStream_t st) {
-  const dim3 b(32, 4);
-  const dim3 g((J.w + 63) / 64, (J.h + 3) / 4);
-  const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.hw_interp) {
-    if (J.patch_half == 5)
-      k_plane_sweep<5, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
-    else if (J.patch_half == 3)
-      k_plane_sweep<3, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
-    else
-      k_plane_sweep<0, true><<<g, b, sm, st>>>(J, color, iter, num_iters);
-  } else {
-    if (J.patch_half == 5)
-      k_plane_sweep<5, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
-    else if (J.patch_half == 3)
-      k_plane_sweep<3, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
-    else
-      k_plane_sweep<0, false><<<g, b, sm, st>>>(J, color, iter, num_iters);
-  }
-  return cudaGetLastError();
+// Dynamic shared memory above the 48 KB default needs an opt-in per kernel.
+template <class K>
+static cudaError_t allow_smem(K* kernel, size_t bytes) {
+  if (bytes <= 32 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t launch_plane_refine(const Job& J, double inv_per_px, int iters, cudaStream_t st) {
-  const dim3 b(32, 4);
-  const size_t sm = pcache_bytes(J.num_src, 128);
-  if (J.hw_interp) {
-    if (J.patch_half == 5)
-      k_plane_refine<5, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-    else if (J.patch_half == 3)
-      k_plane_refine<3, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-    else
-      k_plane_refine<0, true><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-  } else {
-    if (J.patch_half == 5)
-      k_plane_refine<5, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-    else if (J.patch_half == 3)
-      k_plane_refine<3, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-    else
-      k_plane_refine<0, false><<<grid2d(J.w, J.h, b), b, sm, st>>>(J, inv_per_px, iters);
-  }
-  return cudaGetLastError();
+cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, bool hw, int max_src, int* queues, int num_queues,
+                              cudaStream_t st) {
+  const int total = B.start[B.njobs];
+  if (total <= 0) return cudaSuccess;
+  const size_t sm = pcache_bytes(max_src, 128);
+  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+    auto* fn = k_plane_init<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    fn<<<total, dim3(32, 4), sm, st>>>(B, queues, num_queues);
+    return cudaGetLastError();
+  });
 }
 
-cudaError_t launch_plane_output(const Job& J, float* depth, uint8_t* support, float* conf, float* normal,
-                                float* cost, unsigned int* filled, cudaStream_t st) {
-  const dim3 b(32, 8);
-  k_plane_output<<<grid2d(J.w, J.h, b), b, 0, st>>>(J, depth, support, conf, normal, cost, filled);
+cudaError_t plane_sweep_occupancy(int patch_half, bool hw, int max_src, int rows, int* blocks_per_sm) {
+  const size_t sm = pcache_bytes(max_src, 32 * rows);
+  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+    auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 32 * rows, sm);
+  });
+}
+
+cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, bool hw, int max_src,
+                               int rows, int grid, int color, int iter, cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  if (rows < 1 || rows > kMaxTileRows || grid < 1 || total > B.start[B.njobs]) return cudaErrorInvalidValue;
+  const size_t sm = pcache_bytes(max_src, 32 * rows);
+  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+    auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, dim3(32, rows), sm, st>>>(B, total, queue, color, iter);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, bool hw, int max_src, cudaStream_t st) {
+  const int total = B.start[B.njobs];
+  if (total <= 0) return cudaSuccess;
+  const size_t sm = pcache_bytes(max_src, 128);
+  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+    auto* fn = k_plane_refine<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    fn<<<total, dim3(32, 4), sm, st>>>(B);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_plane_output(const PlaneBatch& B, cudaStream_t st) {
+  const int total = B.start[B.njobs];
+  if (total <= 0) return cudaSuccess;
+  k_plane_output<<<total, dim3(32, 4), 0, st>>>(B);
   return cudaGetLastError();
 }
 

@@ -80,7 +80,8 @@ class MvsConfig(C.Structure):
 class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("storage", C.c_int32), ("best_k", C.c_int32), ("refine", C.c_int32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("sampling", C.c_int32), ("prefilter", C.c_int32),
-                ("interp", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("interp", C.c_int32), ("tile_rows", C.c_int32), ("per_view", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -118,7 +119,8 @@ class PointCloudC(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("hypotheses_evaluated", C.c_uint64), ("last_run_ms", C.c_double), ("last_sweep_ms", C.c_double),
-                ("last_sweep_launches", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("last_sweep_launches", C.c_int32), ("tile_rows", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class MvsError(RuntimeError):

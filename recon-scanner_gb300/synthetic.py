@@ -313,6 +313,17 @@ class MvsScene:
     def cameras(self):
         return [self.ref.camera] + [s.camera for s in self.sources]
 
+    @property
+    def views(self):
+        return [self.ref] + list(self.sources)
+
+
+def as_reference(sc: MvsScene, k: int) -> MvsScene:
+    """The same capture with view k as the reference and every other view as
+    a source (view k's truth depth must have been rendered)."""
+    v = sc.views
+    return MvsScene(f"{sc.name}[{k}]", v[k], v[:k] + v[k + 1:], sc.min_depth, sc.max_depth, sc.seed, sc.extra)
+
 
 def sphere_on_backdrop(width=640, height=480, f=600.0, num_sources=4, baseline=0.10,
                        seed=1, device="cpu", noise_sigma=1.0 / 255.0) -> MvsScene:
@@ -406,6 +417,32 @@ def orbit_cameras(n_frames=120, seed=3, resolutions=((640, 480), (1280, 960), (1
         f = f_at_1920 * w / 1920.0
         cams.append(Camera(f, f, w / 2.0, h / 2.0, w, h, R, t))
     return cams
+
+
+def orbit_capture(n_frames=120, n_refs=48, seed=3, src_range=(6, 10), min_baseline=0.015, device="cpu",
+                  noise_sigma=1.0 / 255.0, resolutions=((640, 480), (1280, 960), (1920, 1440))) -> list:
+    """The batched workload: n_refs reference views drawn (seeded) from an
+    orbit capture of the tabletop scene (orbit_cameras: radius 0.30-0.45 m,
+    elevation 10-60 degrees, a seeded mix of resolutions), each with a seeded
+    6-10 sources -- the nearest frames by camera centre at least
+    min_baseline away.  Pinhole cameras.  Returns one MvsScene per reference
+    (frames shared between scenes are rendered once)."""
+    cams = orbit_cameras(n_frames, seed, resolutions)
+    scene = tabletop_scene(2)
+    rng = np.random.default_rng(seed + 5)
+    refs = sorted(int(r) for r in rng.choice(n_frames, n_refs, replace=False))
+    centers = np.stack([c.center() for c in cams])
+    plan = []
+    for r in refs:
+        ns = int(rng.integers(src_range[0], src_range[1] + 1))
+        d = np.linalg.norm(centers - centers[r], axis=1)
+        order = [int(i) for i in np.argsort(d, kind="stable") if i != r and d[i] >= min_baseline]
+        plan.append((r, order[:ns]))
+    need = sorted({r for r, _ in plan} | {i for _, src in plan for i in src})
+    ref_set = {r for r, _ in plan}
+    frames = {i: render(scene, cams[i], noise_sigma, seed * 1000 + i, device, truth=i in ref_set) for i in need}
+    return [MvsScene(f"orbit[{r}]", frames[r], [frames[i] for i in src], 0.10, 0.90, seed, {"frame": r,
+                     "sources": src}) for r, src in plan]
 
 
 def plane_test_scene(width=160, height=120, f=400.0, num_views=5, baseline=0.016, depth=0.35):
