@@ -354,6 +354,46 @@ def agreement(maps_a, maps_b):
     return (float(np.median(d)) if d.size else None), (float(np.quantile(d, 0.95)) if d.size else None)
 
 
+def fuse_capture(M, scenes, maps, rel=0.01, reproj=1.0, min_views=3):
+    """The capture's fusion stage: every map's geometric consistency against
+    the other maps (>= min_views consistent views, reprojection <= reproj px,
+    relative depth <= rel), then FuseDepthMaps of the kept pixels.  Timed on
+    the host around the public calls (maps are host buffers).  Accuracy: the
+    fused points seen by view 0, against its analytic depth."""
+    import numpy as np
+
+    cams = [sc.ref.camera for sc in scenes]
+    poses = [c.pose_array() for c in cams]
+    intr = [c.undistorted().intrinsics_array() for c in cams]
+    t0 = time.perf_counter()
+    keeps = []
+    kept = 0
+    for k in range(len(maps)):
+        _, keep = M.GeometricConsistency(maps, poses, intr, k, rel, reproj, min_views)
+        keeps.append(keep)
+        kept += int(keep.sum())
+    cfg = M.MvsConfig()
+    cloud = M.FuseDepthMaps(maps, poses, intr, cfg, keep_masks=keeps)
+    secs = time.perf_counter() - t0
+    c0 = cams[0]
+    Xc = cloud.positions @ c0.R.T + c0.t
+    ok = Xc[:, 2] > 1e-6
+    u = np.floor(c0.fx * Xc[ok, 0] / Xc[ok, 2] + c0.cx).astype(np.int64)
+    v = np.floor(c0.fy * Xc[ok, 1] / Xc[ok, 2] + c0.cy).astype(np.int64)
+    z = Xc[ok, 2]
+    inside = (u >= 0) & (v >= 0) & (u < c0.width) & (v < c0.height)
+    truth = scenes[0].ref.depth[v[inside], u[inside]]
+    zz = z[inside]
+    vis = np.isfinite(truth) & (np.abs(zz - truth) < 0.05 * truth)  # points on the surface view 0 sees
+    rel_err = np.abs(zz[vis] - truth[vis]) / truth[vis]
+    return {"points": int(cloud.size()), "kept_pixels": kept, "seconds": secs,
+            "thresholds": {"min_views": min_views, "reproj_px": reproj, "rel_depth": rel},
+            "view0_points": int(vis.sum()),
+            "view0_median_rel_err": float(np.median(rel_err)) if rel_err.size else None,
+            "view0_p95_rel_err": float(np.quantile(rel_err, 0.95)) if rel_err.size else None,
+            "timing": "host wall clock: 9 consistency calls + fusion, host buffers in and out"}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -473,12 +513,260 @@ def run_gpu(args):
                          "flop_per_hypothesis": flop_per_hyp},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
             "accuracy": acc, "plain": plain, "clocks": clk.summary()}
+    if WORKLOAD == "c2" and not args.no_fusion:
+        line["fusion"] = fuse_capture(M, scenes, maps)
     if rank == 0 and not args.no_cpu_baseline:
         secs, threads, note = cpu_reference_sample(scenes[0])
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
                                 "sample": note}
     if rank == 0:
         print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# the differentiation and mixed-precision workloads (reports, not the headline)
+# ---------------------------------------------------------------------------
+
+def _pinhole_views(orc, sc):
+    """Undistorted FP32 intensities (orc_undistort, bit-identical to the
+    device remap) and pinhole cameras: what the engine matches."""
+    cams = sc.cameras
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    return [orc.undistort(im, c.intrinsics_array()) for im, c in zip(imgs, cams)], [c.undistorted() for c in cams]
+
+
+def _sph(ang):
+    import numpy as np
+
+    t, p = ang[:, 0], ang[:, 1]
+    return np.stack([np.sin(t) * np.cos(p), np.sin(t) * np.sin(p), np.cos(t)], -1)
+
+
+def run_differentiable(args, n_hyp=10_000):
+    """The C2 views with source poses perturbed by a seeded 0.2 deg rotation
+    and 0.5 mm translation: (1) the adjoint at 10^4 seeded pixels vs FP64
+    central differences of the oracle cost (pixel parameters; pose on 10^3),
+    adjoint throughput; (2) Gauss-Newton vs golden-section refinement
+    accuracy; (3) pose recovery from the PatchMatch map."""
+    import copy
+
+    import numpy as np
+    import torch
+
+    import recon_mvs as M
+    import synthetic as Syn
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    M.load_library()
+    O.build_oracle(ref=False)
+    orc = O.load("oracle")
+    sc = Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device="cuda:0")
+    cams = sc.cameras
+    imgs = [sc.ref.image] + [s.image for s in sc.sources]
+    rng = np.random.default_rng(17)
+
+    def so3(w):
+        th = np.linalg.norm(w)
+        K_ = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+        return np.eye(3) + np.sin(th) / th * K_ + (1 - np.cos(th)) / th ** 2 * K_ @ K_ if th > 1e-12 else np.eye(3)
+
+    def perturb(c, w, tau):
+        c = copy.deepcopy(c)
+        E = so3(np.asarray(w, np.float64))
+        c.R, c.t = E @ c.R, E @ c.t + np.asarray(tau, np.float64)
+        return c
+
+    pert = [cams[0]]
+    for c in cams[1:]:
+        a = rng.normal(size=3)
+        tdir = rng.normal(size=3)
+        pert.append(perturb(c, np.radians(0.2) * a / np.linalg.norm(a), 0.0005 * tdir / np.linalg.norm(tdir)))
+    cfg_kw = dict(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=ITERS, patch_size=K,
+                  subpixel_iterations=4)
+    views = M.ViewArgs.from_cameras(imgs[0], imgs[1:], pert[0], pert[1:])
+    out = {"metric": "differentiation form (C4)", "config": {
+        "workload": f"tabletop {W}x{H}, {S_SRC} sources, poses perturbed 0.2 deg / 0.5 mm (seeded)"}}
+
+    # (1) gradients
+    ys, xs = np.nonzero(np.isfinite(sc.ref.depth[8:-8, 8:-8]))
+    pick = rng.choice(len(xs), n_hyp, replace=False)
+    px, py = (xs[pick] + 8).astype(np.int32), (ys[pick] + 8).astype(np.int32)
+    nt = sc.ref.normal[py, px]
+    depth = sc.ref.depth[py, px] * (1 + rng.uniform(-0.005, 0.005, n_hyp))
+    ang = np.stack([np.arccos(np.clip(nt[:, 2], -1, 1)) + rng.uniform(-0.05, 0.05, n_hyp),
+                    np.arctan2(nt[:, 1], nt[:, 0]) + rng.uniform(-0.05, 0.05, n_hyp)], -1)
+    eng = M.Engine(M.Options(mode=M.MODE_PLANE, best_k=4, device=0))
+    job = eng.stage(views, M.MvsConfig(**cfg_kw), undistort=True)
+    eng.adjoint(job, px[:128], py[:128], depth[:128], ang[:128])  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cost, grad, _, pgrad = eng.adjoint(job, px, py, depth, ang, pose=True)
+    t_adj = time.perf_counter() - t0
+    und, pin = _pinhole_views(orc, Syn.MvsScene("p", Syn.RenderedView(pert[0], imgs[0], None, None),
+                                                [Syn.RenderedView(c, im, None, None) for c, im in
+                                                 zip(pert[1:], imgs[1:])], sc.min_depth, sc.max_depth, 2))
+    vs = O.ViewSet(und[0], und[1:], pin[0], pin[1:])
+    ocfg = O.make_config(num_threads=0, **cfg_kw)
+    oc = lambda d_, a_: orc.plane_costs(vs, ocfg, 4, px, py, 1.0 / d_, _sph(a_))[0]
+    fd = np.zeros((n_hyp, 3))
+    hd = 1e-8 * depth
+    fd[:, 0] = (oc(depth + hd, ang) - oc(depth - hd, ang)) / (2 * hd)
+    for j in (0, 1):
+        e = np.zeros_like(ang)
+        e[:, j] = 1e-8
+        fd[:, 1 + j] = (oc(depth, ang + e) - oc(depth, ang - e)) / 2e-8
+    ok = (cost < 1e29) & np.all(np.isfinite(fd), -1)
+    g, f = grad[ok].astype(np.float64), fd[ok].copy()
+    g[:, 0] *= depth[ok]
+    f[:, 0] *= depth[ok]
+    r = np.linalg.norm(g - f, axis=-1) / np.linalg.norm(f, axis=-1)
+    out["pixel_gradient"] = {"hypotheses": int(ok.sum()), "rel_err_median": float(np.median(r)),
+                             "rel_err_p99": float(np.quantile(r, 0.99)), "frac_le_1e-3": float(np.mean(r <= 1e-3)),
+                             "adjoint_hypotheses_per_s_with_pose": n_hyp / t_adj}
+    m = 1000
+    fdp = np.zeros((m, S_SRC, 6))
+    steps = [1e-8] * 3 + [1e-9] * 3
+    for s_ in range(S_SRC):
+        for j in range(6):
+            w, tau = np.zeros(3), np.zeros(3)
+            (w if j < 3 else tau)[j % 3] = steps[j]
+            c2 = []
+            for sign in (1, -1):
+                cl = list(pin)
+                cl[1 + s_] = perturb(pin[1 + s_], sign * w, sign * tau)
+                v2 = O.ViewSet(und[0], und[1:], cl[0], cl[1:])
+                c2.append(orc.plane_costs(v2, ocfg, 4, px[:m], py[:m], 1.0 / depth[:m], _sph(ang[:m]))[0])
+            fdp[:, s_, j] = (c2[0] - c2[1]) / (2 * steps[j])
+    pg = pgrad[:m].astype(np.float64)
+    sel = np.any(pg != 0, -1) & (cost[:m] < 1e29)[:, None] & np.all(np.isfinite(fdp), -1)
+    gp, fp = pg[sel], fdp[sel]
+    gp[:, 3:] *= 0.4
+    fp[:, 3:] *= 0.4
+    rp = np.linalg.norm(gp - fp, axis=-1) / np.linalg.norm(fp, axis=-1)
+    out["pose_gradient"] = {"pairs": int(sel.sum()), "rel_err_median": float(np.median(rp)),
+                            "rel_err_p99": float(np.quantile(rp, 0.99)), "frac_le_1e-3": float(np.mean(rp <= 1e-3))}
+
+    # (2) + (3): maps on the perturbed poses, pose recovery, maps again
+    def pm(refine, cam_list):
+        e2 = M.Engine(M.Options(mode=M.MODE_PLANE, best_k=4, device=0, refine=refine))
+        v2 = M.ViewArgs.from_cameras(imgs[0], imgs[1:], cam_list[0], cam_list[1:])
+        j2 = e2.stage(v2, M.MvsConfig(**cfg_kw), undistort=True)
+        e2.run(j2)
+        dm = e2.download(j2)
+        ms = e2.stats().last_run_ms
+        e2.close()
+        return dm, ms
+
+    def med(dm):
+        e = np.abs(dm.depth[8:-8, 8:-8].astype(np.float64) - sc.ref.depth[8:-8, 8:-8]) / sc.ref.depth[8:-8, 8:-8]
+        return float(np.nanmedian(e))
+
+    ref_true = {k: pm(k, cams) for k in (1, 2)}
+    out["refinement_true_poses"] = {"golden_section_median_rel_err": med(ref_true[1][0]),
+                                    "gauss_newton_median_rel_err": med(ref_true[2][0]),
+                                    "golden_section_run_ms": ref_true[1][1], "gauss_newton_run_ms": ref_true[2][1]}
+    dm0, _ = pm(2, pert)
+    ys, xs = np.nonzero(np.isfinite(dm0.depth[8:-8:4, 8:-8:4]))
+    qx, qy = (xs * 4 + 8).astype(np.int32), (ys * 4 + 8).astype(np.int32)
+    nn = dm0.normal[qy, qx].astype(np.float64)
+    qa = np.stack([np.arccos(np.clip(nn[:, 2], -1, 1)), np.arctan2(nn[:, 1], nn[:, 0])], -1)
+    t0 = time.perf_counter()
+    poses, hist = eng.recover_poses(job, qx, qy, dm0.depth[qy, qx].astype(np.float64), qa, iterations=15)
+    t_pose = time.perf_counter() - t0
+    eng.close()
+    rec = [cams[0]]
+    for c, p_ in zip(pert[1:], poses):
+        c = copy.deepcopy(c)
+        c.R, c.t = p_[:9].reshape(3, 3).copy(), p_[9:12].copy()
+        rec.append(c)
+
+    def perr(lst):
+        rot = [np.degrees(np.arccos(np.clip((np.trace(c.R @ t.R.T) - 1) / 2, -1, 1))) for c, t in zip(lst, cams[1:])]
+        ctr = [np.linalg.norm(-c.R.T @ c.t + t.R.T @ t.t) * 1e3 for c, t in zip(lst, cams[1:])]
+        return float(np.median(rot)), float(np.median(ctr))
+
+    dm1, _ = pm(2, rec)
+    out["pose_recovery"] = {"pixels": int(len(qx)), "iterations": 15, "seconds": t_pose,
+                            "cost_before": float(hist[0]), "cost_after": float(hist[-1]),
+                            "median_rotation_err_deg_before_after": [perr(pert[1:])[0], perr(rec[1:])[0]],
+                            "median_centre_err_mm_before_after": [perr(pert[1:])[1], perr(rec[1:])[1]],
+                            "map_median_rel_err_perturbed_recovered": [med(dm0), med(dm1)]}
+    print(json.dumps(out))
+
+
+def run_precision(args):
+    """1 + 16 sources at 1920x1440 (40-160 mm baselines) on the tabletop
+    scene: each storage form timed (depth maps/s, one map per step), its
+    error vs analytic truth, and -- on a 160x120 centre crop run by both --
+    its depth / normal difference to the FP64 oracle run of the same search."""
+    import numpy as np
+    import torch
+
+    import recon_mvs as M
+    import synthetic as Syn
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    M.load_library()
+    O.build_oracle(ref=False)
+    orc = O.load("oracle")
+    sc = Syn.tabletop(width=W, height=H, f=F, num_sources=16, seed=2, device="cuda:0", baseline=(0.04, 0.16))
+    views = views_of(M, sc)
+    cfg = config_of(M, sc)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda:0")
+    forms = {"fp32": (M.STORAGE_FP32, 0), "fp16": (M.STORAGE_FP16, 0), "bf16": (M.STORAGE_BF16, 0),
+             "fp16_texture_interp": (M.STORAGE_FP16, 1)}
+    # the crop: same cameras with the principal point shifted
+    cw, ch = 160, 120
+    x0, y0 = W // 2 - cw // 2, H // 2 - ch // 2
+    import copy
+
+    ref_c = copy.deepcopy(sc.ref.camera)
+    ref_c.cx, ref_c.cy, ref_c.width, ref_c.height = ref_c.cx - x0, ref_c.cy - y0, cw, ch
+    crop_img = np.ascontiguousarray(sc.ref.image[y0:y0 + ch, x0:x0 + cw])
+    src_cams = [s.camera for s in sc.sources]
+    src_imgs = [s.image for s in sc.sources]
+    crop_views = M.ViewArgs.from_cameras(crop_img, src_imgs, ref_c, src_cams)
+    und_ref = orc.undistort(crop_img, ref_c.intrinsics_array())
+    und_src = [orc.undistort(im, c.intrinsics_array()) for im, c in zip(src_imgs, src_cams)]
+    vs = O.ViewSet(und_ref, und_src, ref_c.undistorted(), [c.undistorted() for c in src_cams])
+    ocfg = O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=ITERS, patch_size=K,
+                         subpixel_iterations=4, num_threads=0)
+    t0 = time.perf_counter()
+    _, d64, n64, _ = orc.plane_patchmatch(vs, ocfg, best_k=args.best_k, seed=0x5DEECE66D, refine=1)
+    t64 = time.perf_counter() - t0
+    truth_crop = sc.ref.depth[y0:y0 + ch, x0:x0 + cw]
+    out = {"metric": "mixed precision (C5): depth maps/s and errors per storage form",
+           "config": {"workload": f"tabletop {W}x{H}, 16 sources (40-160 mm), {K}x{K}, {ITERS} iterations",
+                      "fp64_oracle_crop": f"{cw}x{ch} centre crop, {t64:.1f} s on the host"}, "forms": {}}
+    b = 8
+    for name, (storage, interp) in forms.items():
+        opts = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=storage, interp=interp, device=0)
+        step_ms, _, _, _, maps, _ = time_form(M, [views], [cfg], opts, args.steps, args.warmup, flush, 1, True)
+        full = accuracy(maps, [sc.ref.depth])
+        eng = M.Engine(opts)
+        j = eng.stage(crop_views, cfg, undistort=True)
+        eng.run(j)
+        dm = eng.download(j)
+        eng.close()
+        a, o, t = dm.depth[b:-b, b:-b].astype(np.float64), d64[b:-b, b:-b].astype(np.float64), truth_crop[b:-b, b:-b]
+        ok = np.isfinite(a) & np.isfinite(o)
+        rel = np.abs(a[ok] - o[ok]) / o[ok]
+        na, no = dm.normal[b:-b, b:-b][ok].astype(np.float64), n64[b:-b, b:-b][ok].astype(np.float64)
+        ang = np.degrees(np.arccos(np.clip(np.sum(na * no, -1), -1, 1)))
+        okt = ok & np.isfinite(t)
+        out["forms"][name] = {
+            "maps_per_s": 1000.0 * len(step_ms) / sum(step_ms), "ms_per_map": statistics.mean(step_ms),
+            "vs_truth": full,
+            "vs_fp64_run": {"median_rel_depth": float(np.median(rel)), "p95_rel_depth": float(np.quantile(rel, 0.95)),
+                            "median_normal_deg": float(np.median(ang)), "p95_normal_deg": float(np.quantile(ang, 0.95)),
+                            "pixels": int(ok.sum())},
+            "crop_vs_truth_median_rel": float(np.median(np.abs(a[okt] - t[okt]) / t[okt])),
+            "fp64_crop_vs_truth_median_rel": float(np.median(np.abs(o[okt] - t[okt]) / t[okt]))}
+    print(json.dumps(out))
 
 
 def main():
@@ -497,7 +785,8 @@ def main():
     ap.add_argument("--interp", type=int, default=None, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3", "c4", "c5"])
+    ap.add_argument("--no-fusion", action="store_true", help="skip the capture's consistency + fusion stage")
     ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
     ap.add_argument("--tile-rows", type=int, default=0, help="sweep tile rows (2, 4, 8); 0 = autotuned")
     args = ap.parse_args()
@@ -506,11 +795,19 @@ def main():
     # the plain FP32 path is timed beside it unless --plain asks for it alone
     if args.plain:
         args.fp16, args.interp, args.per_view = False, 0, True
+    elif args.workload == "c3":
+        # the batched workload is specified all-FP32: batched vs per-view only
+        args.fp16 = False if args.fp16 is None else args.fp16
+        args.interp = 0 if args.interp is None else args.interp
     else:
         args.fp16 = True if args.fp16 is None else args.fp16
         args.interp = 1 if args.interp is None else args.interp
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload == "c4":
+        run_differentiable(args)
+    elif args.workload == "c5":
+        run_precision(args)
     else:
         run_gpu(args)
 

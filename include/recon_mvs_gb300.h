@@ -124,14 +124,18 @@ typedef enum recon_mvs_mode {
 
 typedef enum recon_mvs_storage {
   RECON_MVS_STORAGE_FP32 = 0, /* source images as FP32 textures */
-  RECON_MVS_STORAGE_FP16 = 1  /* FP16 textures: exact for 8-bit input */
+  RECON_MVS_STORAGE_FP16 = 1, /* FP16 textures: exact for 8-bit input */
+  RECON_MVS_STORAGE_BF16 = 2  /* BF16 values (8-bit mantissa; an ablation of FP16) in 16-bit textures,
+                                 read by 2x2 gather and widened exactly; plane mode, interp = 0 only */
 } recon_mvs_storage;
 
 typedef struct recon_mvs_options {
   int32_t mode;       /* recon_mvs_mode */
   int32_t storage;    /* recon_mvs_storage */
   int32_t best_k;     /* plane mode: views averaged per hypothesis, <= 8; 0 = all valid */
-  int32_t refine;     /* plane mode: 1 = golden-section inverse-depth refinement after the sweeps */
+  int32_t refine;     /* plane mode refinement after the sweeps: 0 none; 1 golden-section search of
+                         the inverse depth (the reference's schedule); 2 Gauss-Newton on depth and
+                         normal driven by the adjoint (recon_mvs_job_adjoint) */
   uint64_t seed;      /* plane mode random stream */
   int32_t device;     /* CUDA device ordinal */
   int32_t sampling;   /* plane mode: 0 = pixel-centre windows; 1 = the reference's convention
@@ -318,6 +322,34 @@ RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* vie
  * captured CUDA graph.  Results do not depend on the batching. */
 RECON_API recon_status recon_mvs_job_run(void* ctx, int32_t job);
 RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_t n);
+/* ---- the differentiation form (plane-mode jobs) ---- */
+
+/* Adjoint of the aggregated plane cost at n hypotheses of a staged job: at
+ * integer pixels (px, py), the depth d of the plane on the pixel-centre ray
+ * and its normal as spherical angles angles[2i] = theta, angles[2i+1] = phi
+ * (n = (sin t cos p, sin t sin p, cos t), reference camera frame).  Outputs
+ * per hypothesis: the cost (mean of the best_k view costs, 1e30 invalid),
+ * the gradient d cost / d (d, theta, phi) (3), optionally the Gauss-Newton
+ * matrix (6: upper triangle 00 01 02 11 12 22) and the gradient in every
+ * source's pose (num_src x 6: rotation w then translation tau of the left
+ * perturbation Y' = exp([w]x) Y + tau of source-camera points; zero for views
+ * outside the best_k).  Exact bilinear reads of the staged textures; every
+ * window is recomputed for the reverse pass, never stored.  No counterpart in
+ * the reference (its MVS has no derivatives). */
+RECON_API recon_status recon_mvs_job_adjoint(void* ctx, int32_t job, int32_t n, const int32_t* px, const int32_t* py,
+                                             const double* depth, const double* angles, float* out_cost,
+                                             float* out_grad, float* out_gn, float* out_pose_grad);
+/* Pose recovery: Levenberg-Marquardt on every source pose of a staged job,
+ * minimising each view's mean 1 - NCC over the given hypotheses (held fixed;
+ * every valid view counts, independent of best_k).  The job's source
+ * transforms are updated in place (later runs of the job use them).
+ * out_src_poses (num_src, optional): the refined world -> camera poses;
+ * out_cost (iterations + 1, optional): the summed per-view mean cost before
+ * and after each iteration.  No counterpart in the reference. */
+RECON_API recon_status recon_mvs_job_recover_poses(void* ctx, int32_t job, int32_t n, const int32_t* px,
+                                                   const int32_t* py, const double* depth, const double* angles,
+                                                   int32_t iterations, recon_pose* out_src_poses,
+                                                   double* out_cost);
 /* Copy a finished job's map to the host (synchronises). */
 RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out,
                                               uint32_t* out_filled);

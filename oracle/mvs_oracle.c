@@ -1075,6 +1075,29 @@ static int sample_centre(const uint8_t* img, int w, int h, double cu, double cv,
   return orc_sample_bilinear(img, w, h, cu - 0.5, cv - 0.5, out);
 }
 
+/* SampleBilinear's rules (index == coordinate) on an FP32 image. */
+static int sample_bilinear_f(const float* img, int w, int h, double u, double v, double* out) {
+  if (u < 0.0 || v < 0.0 || u > (double)(w - 1) || v > (double)(h - 1)) return 0;
+  const int x0 = (int)floor(u), y0 = (int)floor(v);
+  const int x1 = x0 + 1 < w ? x0 + 1 : w - 1, y1 = y0 + 1 < h ? y0 + 1 : h - 1;
+  const double fx = u - x0, fy = v - y0;
+  const double top = img[(size_t)y0 * w + x0] * (1.0 - fx) + img[(size_t)y0 * w + x1] * fx;
+  const double bot = img[(size_t)y1 * w + x0] * (1.0 - fx) + img[(size_t)y1 * w + x1] * fx;
+  *out = top * (1.0 - fy) + bot * fy;
+  return 1;
+}
+
+/* Source sample k at (u, v): 8-bit or FP32 image, pixel-centre or the
+ * reference's index == coordinate convention. */
+static int sample_source(const orc_views* v, int k, double u, double vv, int half_pixel, double* out) {
+  if (v->src_f != NULL) {
+    const double o = half_pixel ? 0.0 : 0.5;
+    return sample_bilinear_f(v->src_f[k], v->src_w[k], v->src_h[k], u - o, vv - o, out);
+  }
+  if (half_pixel) return orc_sample_bilinear(v->src[k], v->src_w[k], v->src_h[k], u, vv, out);
+  return sample_centre(v->src[k], v->src_w[k], v->src_h[k], u, vv, out);
+}
+
 orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32_t best_k,
                                 int32_t x, int32_t y, double inv_depth, const double n[3],
                                 int32_t half_pixel) {
@@ -1123,10 +1146,14 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
         const int rx = x + dx, ry = y + dy;
         double vr = 0.0;
         if (half_pixel) {
-          if (!orc_sample_bilinear(v->ref, v->ref_w, v->ref_h, rx + 0.5, ry + 0.5, &vr)) continue;
+          if (v->ref_f != NULL) {
+            if (!sample_bilinear_f(v->ref_f, v->ref_w, v->ref_h, rx + 0.5, ry + 0.5, &vr)) continue;
+          } else if (!orc_sample_bilinear(v->ref, v->ref_w, v->ref_h, rx + 0.5, ry + 0.5, &vr)) {
+            continue;
+          }
         } else {
           if (rx < 0 || ry < 0 || rx > v->ref_w - 1 || ry > v->ref_h - 1) continue;
-          vr = v->ref[(size_t)ry * v->ref_w + rx];
+          vr = v->ref_f != NULL ? (double)v->ref_f[(size_t)ry * v->ref_w + rx] : v->ref[(size_t)ry * v->ref_w + rx];
         }
         const double rp[3] = {(rx + 0.5 - kr->cx) / kr->fx, (ry + 0.5 - kr->cy) / kr->fy, 1.0};
         const double nd = n[0] * rp[0] + n[1] * rp[1] + n[2] * rp[2];
@@ -1140,11 +1167,7 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
         const double su = ks->fx * (Xs[0] / Xs[2]) + ks->cx;
         const double sv = ks->fy * (Xs[1] / Xs[2]) + ks->cy;
         double vs = 0.0;
-        if (half_pixel) {
-          if (!orc_sample_bilinear(v->src[k], v->src_w[k], v->src_h[k], su, sv, &vs)) continue;
-        } else if (!sample_centre(v->src[k], v->src_w[k], v->src_h[k], su, sv, &vs)) {
-          continue;
-        }
+        if (!sample_source(v, k, su, sv, half_pixel, &vs)) continue;
         sr += vr;
         ss += vs;
         srr += vr * vr;
@@ -1187,17 +1210,50 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
   return res;
 }
 
+typedef struct {
+  const orc_views* v;
+  const orc_config* cfg;
+  int32_t best_k, i0, i1, half_pixel;
+  const int32_t *px, *py;
+  const double *inv, *normals;
+  double* out_cost;
+  int32_t* out_valid_views;
+  double* out_view_cost;
+} plane_costs_task;
+
+static void* plane_costs_run(void* arg) {
+  const plane_costs_task* T = (const plane_costs_task*)arg;
+  for (int32_t i = T->i0; i < T->i1; ++i) {
+    const orc_plane_result r =
+        orc_plane_cost(T->v, T->cfg, T->best_k, T->px[i], T->py[i], T->inv[i], &T->normals[3 * i], T->half_pixel);
+    T->out_cost[i] = r.cost;
+    T->out_valid_views[i] = r.valid_views;
+    if (T->out_view_cost)
+      for (int k = 0; k < T->v->num_src; ++k) T->out_view_cost[(size_t)i * T->v->num_src + k] = r.view_cost[k];
+  }
+  return NULL;
+}
+
+/* Independent hypotheses: split over cfg->num_threads threads (0 = all). */
 void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, int32_t n,
                      const int32_t* px, const int32_t* py, const double* inv,
                      const double* normals, double* out_cost, int32_t* out_valid_views,
                      double* out_view_cost, int32_t half_pixel) {
-  for (int32_t i = 0; i < n; ++i) {
-    const orc_plane_result r = orc_plane_cost(v, cfg, best_k, px[i], py[i], inv[i], &normals[3 * i], half_pixel);
-    out_cost[i] = r.cost;
-    out_valid_views[i] = r.valid_views;
-    if (out_view_cost)
-      for (int k = 0; k < v->num_src; ++k) out_view_cost[(size_t)i * v->num_src + k] = r.view_cost[k];
+  int threads = cfg->num_threads > 0 ? cfg->num_threads : (int)sysconf(_SC_NPROCESSORS_ONLN);
+  if (threads < 1) threads = 1;
+  if (threads > n / 64 + 1) threads = n / 64 + 1;
+  plane_costs_task* tasks = (plane_costs_task*)malloc(sizeof(plane_costs_task) * (size_t)threads);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+  for (int t = 0; t < threads; ++t) {
+    plane_costs_task T = {v, cfg, best_k, (int32_t)((long long)n * t / threads),
+                          (int32_t)((long long)n * (t + 1) / threads), half_pixel, px, py, inv, normals,
+                          out_cost, out_valid_views, out_view_cost};
+    tasks[t] = T;
+    pthread_create(&th[t], NULL, plane_costs_run, &tasks[t]);
   }
+  for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+  free(th);
+  free(tasks);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1309,4 +1365,348 @@ void orc_undistort(const uint8_t* img, int32_t w, int32_t h, const orc_intrinsic
       out[(size_t)j * w + i] = (float)val;
     }
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Plane-mode PatchMatch in FP64 (no reference counterpart)                  */
+/* ------------------------------------------------------------------------ */
+/* The GPU engine's plane-mode search restated with every cost evaluated in
+ * FP64 by orc_plane_cost (pixel-centre windows): the same red-black
+ * schedule, the same 8 adaptive propagation regions and 5 refinement
+ * hypotheses per half-sweep, the same counter-based random streams
+ * (splitmix64 finaliser), and the same golden-section refinement.  Random
+ * unit vectors use cos / sin in FP64 where the GPU uses its FP32 intrinsics,
+ * so the two runs draw the same hypotheses up to ~1e-6 in the normals.  It is
+ * the FP64 run the mixed-precision forms are measured against. */
+
+static uint64_t pm_mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+typedef struct {
+  uint64_t s;
+} pm_rng;
+static float pm_uniform(pm_rng* g) {
+  g->s = pm_mix64(g->s);
+  return (float)(uint32_t)(g->s >> 40) * (1.0f / 16777216.0f);
+}
+static float pm_sym(pm_rng* g) { return pm_uniform(g) * 2.0f - 1.0f; }
+static pm_rng pm_pixel_rng(uint64_t seed, int idx, int iter, int salt) {
+  pm_rng g;
+  g.s = pm_mix64(seed ^ ((uint64_t)idx * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(iter + 1) << 40) ^
+                 ((uint64_t)salt << 56));
+  return g;
+}
+
+static void pm_random_normal(pm_rng* g, double rx, double ry, double n[3]) {
+  const double rn = 1.0 / sqrt(rx * rx + ry * ry + 1.0);
+  for (int t = 0; t < 8; ++t) {
+    const double z = pm_sym(g);
+    const double phi = 6.28318530718 * pm_uniform(g);
+    const double r = sqrt(fmax(0.0, 1.0 - z * z));
+    double a = r * cos(phi), b = r * sin(phi), c = z;
+    double d = (a * rx + b * ry + c) * rn;
+    if (d > 0.0) {
+      a = -a;
+      b = -b;
+      c = -c;
+      d = -d;
+    }
+    if (d < -0.2) {
+      n[0] = a;
+      n[1] = b;
+      n[2] = c;
+      return;
+    }
+  }
+  n[0] = 0.0;
+  n[1] = 0.0;
+  n[2] = -1.0;
+}
+
+static void pm_perturb_normal(pm_rng* g, double rx, double ry, double scale, double n[3]) {
+  double a = n[0] + scale * pm_sym(g), b = n[1] + scale * pm_sym(g), c = n[2] + scale * pm_sym(g);
+  const double inv = 1.0 / sqrt(a * a + b * b + c * c);
+  a *= inv;
+  b *= inv;
+  c *= inv;
+  const double rn = 1.0 / sqrt(rx * rx + ry * ry + 1.0);
+  if ((a * rx + b * ry + c) * rn < -0.2) {
+    n[0] = a;
+    n[1] = b;
+    n[2] = c;
+  }
+}
+
+typedef struct {
+  const orc_views* v;
+  const orc_config* cfg;
+  int best_k;
+  uint64_t seed;
+  double rho_min, rho_max, inv_per_px;
+  double* hyp; /* rho, nx, ny, nz per pixel */
+  double* cost;
+  int32_t* support;
+  int stage; /* 0 init, 1 sweep, 2 refine */
+  int color, iter;
+  int y0, y1;
+} pm_task;
+
+static double pm_eval(const pm_task* T, int x, int y, double rx, double ry, double rho, const double n[3],
+                      int32_t* support) {
+  *support = 0;
+  if (!(rho > 0.0) || rho < T->rho_min || rho > T->rho_max) return 1e30;
+  const double kappa = n[0] * rx + n[1] * ry + n[2];
+  if (!(kappa < -0.05 * sqrt(rx * rx + ry * ry + 1.0))) return 1e30;
+  const orc_plane_result r = orc_plane_cost(T->v, T->cfg, T->best_k, x, y, rho, n, 0);
+  *support = r.valid_views;
+  return r.cost;
+}
+
+static const signed char pm_near[4][7][2] = {
+    {{0, -1}, {-1, -2}, {1, -2}, {-2, -3}, {2, -3}, {-3, -4}, {3, -4}},
+    {{0, 1}, {-1, 2}, {1, 2}, {-2, 3}, {2, 3}, {-3, 4}, {3, 4}},
+    {{-1, 0}, {-2, -1}, {-2, 1}, {-3, -2}, {-3, 2}, {-4, -3}, {-4, 3}},
+    {{1, 0}, {2, -1}, {2, 1}, {3, -2}, {3, 2}, {4, -3}, {4, 3}}};
+
+static void pm_pixel(const pm_task* T, int x, int y) {
+  const orc_views* v = T->v;
+  const orc_intrinsics* k = v->ref_intr;
+  const int W = v->ref_w, H = v->ref_h;
+  const int idx = y * W + x;
+  const double rx = (x + 0.5 - k->cx) / k->fx, ry = (y + 0.5 - k->cy) / k->fy;
+  double* h = T->hyp + 4 * (size_t)idx;
+  if (T->stage == 0) {
+    pm_rng g = pm_pixel_rng(T->seed, idx, -1, 1);
+    const double rho = T->rho_min + (T->rho_max - T->rho_min) * pm_uniform(&g);
+    double n[3];
+    pm_random_normal(&g, rx, ry, n);
+    int32_t sup;
+    T->cost[idx] = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+    T->support[idx] = sup;
+    h[0] = rho;
+    h[1] = n[0];
+    h[2] = n[1];
+    h[3] = n[2];
+    return;
+  }
+  if (T->stage == 1) {
+    double cur[4] = {h[0], h[1], h[2], h[3]};
+    double cur_cost = T->cost[idx];
+    int32_t cur_sup = T->support[idx];
+    for (int r = 0; r < 8; ++r) {
+      int best_n = -1;
+      double best_c = 1e30;
+      const int cnt = r < 4 ? 7 : 11;
+      for (int q = 0; q < cnt; ++q) {
+        int nx_, ny_;
+        if (r < 4) {
+          nx_ = x + pm_near[r][q][0];
+          ny_ = y + pm_near[r][q][1];
+        } else {
+          const int d = r - 4, off = 3 + 2 * q;
+          const int sx = d == 2 ? -1 : (d == 3 ? 1 : 0), sy = d == 0 ? -1 : (d == 1 ? 1 : 0);
+          nx_ = x + sx * off;
+          ny_ = y + sy * off;
+        }
+        if (nx_ < 0 || ny_ < 0 || nx_ >= W || ny_ >= H) continue;
+        const double c = T->cost[ny_ * W + nx_];
+        if (c < best_c) {
+          best_c = c;
+          best_n = ny_ * W + nx_;
+        }
+      }
+      if (best_n < 0 || best_c >= 1e30) continue;
+      const double* hn = T->hyp + 4 * (size_t)best_n;
+      const int nxp = best_n % W, nyp = best_n / W;
+      const double rxn = (nxp + 0.5 - k->cx) / k->fx, ryn = (nyp + 0.5 - k->cy) / k->fy;
+      const double kn = hn[1] * rxn + hn[2] * ryn + hn[3];
+      const double kp = hn[1] * rx + hn[2] * ry + hn[3];
+      const double rho = (kn < 0.0 && kp < 0.0) ? hn[0] * kp / kn : -1.0;
+      if (!(rho > 0.0)) continue;
+      if (rho == cur[0] && hn[1] == cur[1] && hn[2] == cur[2] && hn[3] == cur[3]) continue;
+      const double n[3] = {hn[1], hn[2], hn[3]};
+      int32_t sup;
+      const double c = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+      if (c < cur_cost) {
+        cur_cost = c;
+        cur[0] = rho;
+        cur[1] = hn[1];
+        cur[2] = hn[2];
+        cur[3] = hn[3];
+        cur_sup = sup;
+      }
+    }
+    pm_rng g = pm_pixel_rng(T->seed, idx, T->iter, 2 + T->color);
+    const double scale = ldexp(1.0, -T->iter);
+    const double span = T->rho_max - T->rho_min;
+    for (int q = 0; q < 5; ++q) {
+      double rho = cur[0], n[3] = {cur[1], cur[2], cur[3]};
+      if (q == 0) {
+        rho = T->rho_min + span * pm_uniform(&g);
+        pm_random_normal(&g, rx, ry, n);
+      } else if (q == 4) {
+        if (n[0] == 0.0 && n[1] == 0.0) continue;
+        n[0] = 0.0;
+        n[1] = 0.0;
+        n[2] = -1.0;
+      } else {
+        if (q & 1) rho = cur[0] + 0.25 * span * scale * pm_sym(&g);
+        if (q & 2) pm_perturb_normal(&g, rx, ry, 0.5 * scale, n);
+      }
+      int32_t sup;
+      const double c = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+      if (c < cur_cost) {
+        cur_cost = c;
+        cur[0] = rho;
+        cur[1] = n[0];
+        cur[2] = n[1];
+        cur[3] = n[2];
+        cur_sup = sup;
+      }
+    }
+    for (int i = 0; i < 4; ++i) h[i] = cur[i];
+    T->cost[idx] = cur_cost;
+    T->support[idx] = cur_sup;
+    return;
+  }
+  /* stage 2: golden-section refinement of the inverse depth along the normal */
+  const double c0 = T->cost[idx];
+  if (!(c0 < 1e29)) return;
+  const double n[3] = {h[1], h[2], h[3]};
+  double best_d = h[0], best_c = c0;
+  int32_t best_s = T->support[idx];
+  double lo = fmax(T->rho_min, best_d - T->inv_per_px);
+  double hi = fmin(T->rho_max, best_d + T->inv_per_px);
+  if (hi > lo) {
+    const double inv_phi = 0.618033988749895;
+    double c1 = hi - inv_phi * (hi - lo), c2 = lo + inv_phi * (hi - lo);
+    int32_t s1, s2, sm;
+    double f1 = pm_eval(T, x, y, rx, ry, c1, n, &s1), f2 = pm_eval(T, x, y, rx, ry, c2, n, &s2);
+    for (int q = 0; q < T->cfg->subpixel_iterations; ++q) {
+      if (f1 < f2) {
+        hi = c2;
+        c2 = c1;
+        f2 = f1;
+        s2 = s1;
+        c1 = hi - inv_phi * (hi - lo);
+        f1 = pm_eval(T, x, y, rx, ry, c1, n, &s1);
+      } else {
+        lo = c1;
+        c1 = c2;
+        f1 = f2;
+        s1 = s2;
+        c2 = lo + inv_phi * (hi - lo);
+        f2 = pm_eval(T, x, y, rx, ry, c2, n, &s2);
+      }
+    }
+    const double mid = 0.5 * (lo + hi);
+    const double fm = pm_eval(T, x, y, rx, ry, mid, n, &sm);
+    if (fm < best_c) {
+      best_c = fm;
+      best_d = mid;
+      best_s = sm;
+    }
+    if (f1 < best_c) {
+      best_c = f1;
+      best_d = c1;
+      best_s = s1;
+    }
+    if (f2 < best_c) {
+      best_c = f2;
+      best_d = c2;
+      best_s = s2;
+    }
+  }
+  h[0] = best_d;
+  T->cost[idx] = best_c;
+  T->support[idx] = best_s;
+}
+
+static void* pm_task_run(void* arg) {
+  const pm_task* T = (const pm_task*)arg;
+  const int W = T->v->ref_w;
+  for (int y = T->y0; y < T->y1; ++y)
+    for (int x = 0; x < W; ++x) {
+      if (T->stage == 1 && ((x + y) & 1) != T->color) continue;
+      pm_pixel(T, x, y);
+    }
+  return NULL;
+}
+
+static void pm_run_stage(const pm_task* base, int threads) {
+  const int H = base->v->ref_h;
+  const int count = threads < H ? threads : H;
+  pm_task* tasks = (pm_task*)malloc(sizeof(pm_task) * (size_t)count);
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)count);
+  for (int b = 0; b < count; ++b) {
+    tasks[b] = *base;
+    tasks[b].y0 = (int)((long long)H * b / count);
+    tasks[b].y1 = (int)((long long)H * (b + 1) / count);
+    pthread_create(&th[b], NULL, pm_task_run, &tasks[b]);
+  }
+  for (int b = 0; b < count; ++b) pthread_join(th[b], NULL);
+  free(th);
+  free(tasks);
+}
+
+uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                              int32_t refine, float* depth, float* normal, float* cost_out) {
+  const size_t n = (size_t)v->ref_w * v->ref_h;
+  for (size_t i = 0; i < n; ++i) {
+    depth[i] = NAN;
+    if (normal) normal[3 * i] = normal[3 * i + 1] = normal[3 * i + 2] = 0.0f;
+    if (cost_out) cost_out[i] = 1e30f;
+  }
+  double inv_min, inv_max, baseline;
+  if (!orc_pm_prepare(v, cfg, &inv_min, &inv_max, &baseline)) return 0;
+  const orc_intrinsics* k = v->ref_intr;
+  pm_task T;
+  memset(&T, 0, sizeof(T));
+  T.v = v;
+  T.cfg = cfg;
+  T.best_k = best_k;
+  T.seed = seed;
+  T.rho_min = inv_min;
+  T.rho_max = inv_max;
+  T.inv_per_px = 1.0 / (0.5 * (k->fx + k->fy) * baseline);
+  T.hyp = (double*)malloc(sizeof(double) * 4 * n);
+  T.cost = (double*)malloc(sizeof(double) * n);
+  T.support = (int32_t*)malloc(sizeof(int32_t) * n);
+  int threads = cfg->num_threads;
+  if (threads <= 0) threads = (int)sysconf(_SC_NPROCESSORS_ONLN);
+  if (threads <= 0) threads = 1;
+  T.stage = 0;
+  pm_run_stage(&T, threads);
+  for (int it = 0; it < cfg->iterations; ++it)
+    for (int c = 0; c < 2; ++c) {
+      T.stage = 1;
+      T.iter = it;
+      T.color = c;
+      pm_run_stage(&T, threads);
+    }
+  if (refine && cfg->subpixel_iterations > 0) {
+    T.stage = 2;
+    pm_run_stage(&T, threads);
+  }
+  uint32_t filled = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const double rho = T.hyp[4 * i];
+    if (T.cost[i] < 1e29 && rho > 0.0) {
+      const double d = 1.0 / rho;
+      if (d >= cfg->min_depth_m && d <= cfg->max_depth_m) {
+        depth[i] = (float)d;
+        ++filled;
+      }
+    }
+    if (normal)
+      for (int c = 0; c < 3; ++c) normal[3 * i + c] = (float)T.hyp[4 * i + 1 + c];
+    if (cost_out) cost_out[i] = (float)T.cost[i];
+  }
+  free(T.hyp);
+  free(T.cost);
+  free(T.support);
+  return filled;
 }

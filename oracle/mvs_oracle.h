@@ -96,6 +96,10 @@ typedef struct orc_views {
   const orc_intrinsics* src_intr;
   int32_t num_src_intr;
   const int32_t* source_indices;
+  /* Optional FP32 intensities (e.g. undistorted images) read instead of the
+   * 8-bit ones by orc_plane_cost and orc_plane_patchmatch; NULL = 8-bit. */
+  const float* ref_f;
+  const float* const* src_f;
 } orc_views;
 
 typedef struct orc_ncc_result {
@@ -210,6 +214,15 @@ void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, 
                      const int32_t* px, const int32_t* py, const double* inv,
                      const double* normals, double* out_cost, int32_t* out_valid_views,
                      double* out_view_cost, int32_t half_pixel);
+
+/* Plane-mode PatchMatch with every cost in FP64 (orc_plane_cost, pixel-centre
+ * windows): the GPU engine's red-black search -- 8 adaptive propagation
+ * regions, 5 refinement hypotheses per half-sweep, counter-based random
+ * streams, golden-section refinement -- restated as the FP64 run the
+ * mixed-precision forms are compared with.  depth NaN where invalid; normal
+ * (optional) 3 floats per pixel; cost (optional).  Returns the filled count. */
+uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                              int32_t refine, float* depth, float* normal, float* cost);
 
 /* Geometric consistency (spec: shaders/vulkan/recon_mvs_consistency.comp:94-140
  * with the strict transform of shaders/common/gpu_algo.h:537-538, plus a

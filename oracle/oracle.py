@@ -75,6 +75,7 @@ class Views(C.Structure):
         ("ref_pose", C.POINTER(Pose)), ("src_poses", C.POINTER(Pose)), ("num_src_poses", C.c_int32),
         ("ref_intr", C.POINTER(Intrinsics)), ("src_intr", C.POINTER(Intrinsics)), ("num_src_intr", C.c_int32),
         ("source_indices", C.POINTER(C.c_int32)),
+        ("ref_f", C.POINTER(C.c_float)), ("src_f", C.POINTER(C.POINTER(C.c_float))),
     ]
 
 
@@ -119,6 +120,14 @@ class ViewSet:
 
     def __init__(self, ref_img, src_imgs, ref_cam, src_cams, source_indices=None,
                  all_poses=None, intrinsics="relative"):
+        # FP32 images (e.g. undistorted intensities) are kept for the plane
+        # cost and the plane search; the 8-bit copies are their rounding
+        self.is_float = np.issubdtype(np.asarray(ref_img).dtype, np.floating)
+        if self.is_float:
+            self.ref_f = np.ascontiguousarray(ref_img, np.float32)
+            self.srcs_f = [np.ascontiguousarray(s, np.float32) for s in src_imgs]
+            ref_img = np.clip(np.round(self.ref_f), 0, 255)
+            src_imgs = [np.clip(np.round(s), 0, 255) for s in self.srcs_f]
         self.ref = np.ascontiguousarray(ref_img, np.uint8)
         self.srcs = [np.ascontiguousarray(s, np.uint8) for s in src_imgs]
         n = len(self.srcs)
@@ -144,6 +153,10 @@ class ViewSet:
             C.pointer(self.ref_pose), C.cast(self.poses, C.POINTER(Pose)), len(all_poses),
             C.pointer(self.ref_intr), C.cast(self.intr, C.POINTER(Intrinsics)), len(intr),
             _ptr(self.source_indices, C.c_int32))
+        if self.is_float:
+            self.src_f_ptrs = (C.POINTER(C.c_float) * n)(*[_ptr(s, C.c_float) for s in self.srcs_f])
+            self.struct.ref_f = _ptr(self.ref_f, C.c_float)
+            self.struct.src_f = C.cast(self.src_f_ptrs, C.POINTER(C.POINTER(C.c_float)))
 
     @property
     def shape(self):
@@ -220,6 +233,9 @@ def load(which: str = "oracle") -> "Checker":
                                                    C.POINTER(C.c_float)]
         lib.orc_undistort.argtypes = [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.POINTER(Intrinsics),
                                       C.POINTER(C.c_float)]
+        lib.orc_plane_patchmatch.restype = C.c_uint32
+        lib.orc_plane_patchmatch.argtypes = [V, P, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_float),
+                                             C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.orc_xorshift_next.restype = C.c_uint32
         lib.orc_xorshift_next.argtypes = [C.POINTER(C.c_uint64)]
         lib.orc_apply_distortion.argtypes = [C.POINTER(Intrinsics), C.c_double, C.c_double, d, d]
@@ -373,6 +389,18 @@ class Checker:
                                  _ptr(cost, C.c_double), _ptr(vv, C.c_int32), _ptr(view_cost, C.c_double),
                                  int(half_pixel))
         return cost, vv, view_cost
+
+    def plane_patchmatch(self, vs: ViewSet, cfg: Config, best_k=4, seed=0x5DEECE66D, refine=1):
+        """The plane-mode search with FP64 costs.  Returns (filled, depth,
+        normal HxWx3, cost)."""
+        h, w = vs.ref.shape
+        depth = np.zeros((h, w), np.float32)
+        normal = np.zeros((h, w, 3), np.float32)
+        cost = np.zeros((h, w), np.float32)
+        filled = self.lib.orc_plane_patchmatch(C.byref(vs.struct), C.byref(cfg), int(best_k), int(seed), int(refine),
+                                               _ptr(depth, C.c_float), _ptr(normal, C.c_float),
+                                               _ptr(cost, C.c_float))
+        return int(filled), depth, normal, cost
 
     def undistort(self, img, intr):
         img = np.ascontiguousarray(img, np.uint8)

@@ -25,6 +25,7 @@
 namespace rmvs {
 
 constexpr int kMaxSources = 32;
+constexpr int kMaxBestK = 8;  // views averaged per hypothesis, at most
 constexpr float kCostInf = 1e30f;
 
 // ---------------------------------------------------------------------------
@@ -151,6 +152,9 @@ struct SrcView {
   double bd[3];
 };
 
+// Source read modes of the plane-mode kernels (Job::src_mode).
+constexpr int kSrcExact = 0, kSrcTex = 1, kSrcBf16 = 2;
+
 // One reference view: its image, camera and search state.
 struct Job {
   int w, h, num_src;
@@ -169,9 +173,11 @@ struct Job {
   // (window at x + 0.5 + dx with index == coordinate, i.e. the 2x2 box image,
   // source index == coordinate)
   int half_pixel;
-  // plane mode interpolation: 0 = exact FP32 bilinear from a 2x2 gather;
-  // 1 = the texture unit's bilinear filter (8-bit fixed-point weights)
-  int hw_interp;
+  // plane mode source reads: 0 = exact FP32 bilinear from a 2x2 gather of an
+  // FP32 / FP16 texture; 1 = the texture unit's bilinear filter (8-bit
+  // fixed-point weights); 2 = exact FP32 bilinear from a 2x2 gather of BF16
+  // bits held in a 16-bit unsigned texture
+  int src_mode;
   const float* pref;     // the plane-mode reference window image: ref or ref_box
   const SrcView* src;    // num_src entries (device memory)
   // plane-mode state
@@ -193,7 +199,8 @@ struct Job {
   const float* seed_depth;  // optional per-32-px-cell seed depth, seed_gx cells per row
   int seed_gx;
   int iterations;           // red-black iterations of this job
-  int refine_iters;         // golden-section steps; 0 = no refinement
+  int refine_iters;         // refinement steps; 0 = no refinement
+  int refine_mode;          // 1 = golden-section on the inverse depth, 2 = Gauss-Newton on (d, theta, phi)
   float inv_per_px;         // refinement half-range: 1 px of disparity in inverse depth
   float* out_depth;
   uint8_t* out_support;

@@ -76,13 +76,42 @@ __device__ __forceinline__ bool source_centre(const SrcView& S, const ff P[3], f
   return true;
 }
 
+// How plane-mode kernels read source texels (a template parameter, the
+// constants kSrcExact / kSrcTex / kSrcBf16):
+//   kSrcExact -- FP32 or FP16 texture, 2x2 gather, exact FP32 bilinear;
+//   kSrcTex   -- the texture unit's bilinear filter (8-bit fixed-point weights);
+//   kSrcBf16  -- BF16 values in a 16-bit unsigned texture (the texture unit has
+//                no BF16 format), 2x2 gather of the raw bits widened exactly to
+//                FP32, exact FP32 bilinear.
+
+// The 2x2 footprint at gather coordinate (x, y); order (x0,y1) (x1,y1) (x1,y0) (x0,y0).
+template <int kMode>
+__device__ __forceinline__ float4 gather4(cudaTextureObject_t tex, float x, float y) {
+  if constexpr (kMode == kSrcBf16) {
+    const ushort4 g = tex2Dgather<ushort4>(tex, x, y, 0);
+    return make_float4(__uint_as_float((unsigned)g.x << 16), __uint_as_float((unsigned)g.y << 16),
+                       __uint_as_float((unsigned)g.z << 16), __uint_as_float((unsigned)g.w << 16));
+  } else {
+    return tex2Dgather<float4>(tex, x, y, 0);
+  }
+}
+
 // Bilinear read of the 2x2 footprint whose top-left texel is (x0, y0),
-// given as float texel indices; gather order is (x0,y1) (x1,y1) (x1,y0) (x0,y0).
+// given as float texel indices.
+template <int kMode = kSrcExact>
 __device__ __forceinline__ float bilinear(cudaTextureObject_t tex, float x0, float y0, float fx, float fy) {
-  const float4 g = tex2Dgather<float4>(tex, x0 + 1.0f, y0 + 1.0f, 0);
+  const float4 g = gather4<kMode>(tex, x0 + 1.0f, y0 + 1.0f);
   const float top = fmaf(fx, g.z - g.w, g.w);
   const float bot = fmaf(fx, g.y - g.x, g.x);
   return fmaf(fy, bot - top, top);
+}
+
+// Kahan-compensated accumulation: sum += v with the running compensation c.
+__device__ __forceinline__ void kahan_add(float& sum, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(sum, y);
+  c = __fsub_rn(__fsub_rn(t, sum), y);
+  sum = t;
 }
 
 __device__ __forceinline__ ViewResult ncc_from_moments(float n, float sr, float srr, float ss, float sss, float srs,
@@ -190,12 +219,13 @@ __device__ __forceinline__ bool make_plane_hyp(const Job& J, float rx, float ry,
   return true;
 }
 
-template <bool kFull, bool kHw>
+template <bool kFull, int kMode>
 __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int x, int y, int iu, int iv, float fu,
                                              float fv, float A0, float A1, float B0, float B1, float c0, float c1,
                                              const PlaneHyp& hp, float rmean, float sc, float* acc, float* cnt) {
   const int h = J.patch_half;
   float sr = 0.f, srr = 0.f, ss = 0.f, sss = 0.f, srs = 0.f, n = 0.f;
+  float cr = 0.f, crr = 0.f, cs = 0.f, css = 0.f, crs = 0.f;  // Kahan compensations across rows
   const float bu = (float)iu, bv = (float)iv;
   const float umax = (float)(S.w - 1 - iu), vmax = (float)(S.h - 1 - iv);
   const float umin = (float)(-iu), vmin = (float)(-iv);
@@ -222,8 +252,8 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
       }
       if (ok) {
         const float flu = floorf(tu), flv = floorf(tv);
-        const float sv = (kHw ? tex2D<float>(S.tex_lin, bu + tu + 0.5f, bv + tv + 0.5f)
-                              : bilinear(S.tex, bu + flu, bv + flv, tu - flu, tv - flv)) - sc;
+        const float sv = (kMode == kSrcTex ? tex2D<float>(S.tex_lin, bu + tu + 0.5f, bv + tv + 0.5f)
+                                           : bilinear<kMode>(S.tex, bu + flu, bv + flv, tu - flu, tv - flv)) - sc;
         const float rv = __ldg(rrow + dx) - rmean;
         r_s += sv;
         r_ss = fmaf(sv, sv, r_ss);
@@ -239,11 +269,11 @@ __device__ __forceinline__ void plane_window(const Job& J, const SrcView& S, int
       nv += B0;
       nr += hp.ex;
     }
-    ss += r_s;
-    sss += r_ss;
-    srs += r_rs;
-    sr += r_r;
-    srr += r_rr;
+    kahan_add(ss, cs, r_s);
+    kahan_add(sss, css, r_ss);
+    kahan_add(srs, crs, r_rs);
+    kahan_add(sr, cr, r_r);
+    kahan_add(srr, crr, r_rr);
     n += r_n;
   }
   acc[0] = sr;
@@ -300,7 +330,7 @@ struct TileRef {
 // rounding (FMA pipe): m = t' + 1.5*2^23 rounds t' = t - 0.5 to the nearest
 // integer, i.e. floor(t); at exact ties the footprint shifts by one texel
 // with weight 1, which reads the same value (bilinear is continuous).
-template <int H, bool kHw, class Row>
+template <int H, int kMode, class Row>
 __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Row& row,
                                           float& den, float& nu, float& nv, float c0, float A0, float B0, float fum,
                                           float fvm, float gxo, float gyo, float cuo, float cvo, float rmean, float sc,
@@ -310,7 +340,7 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureOb
   for (int k = 0; k <= 2 * H; ++k) {
     const float rinv = rcp_approx(den);
     float sv;
-    if constexpr (kHw) {
+    if constexpr (kMode == kSrcTex) {
       // texture coordinate of index coordinate t: t + 0.5
       sv = tex2D<float>(tex_lin, fmaf(nu, rinv, cuo), fmaf(nv, rinv, cvo)) - sc;
     } else {
@@ -320,7 +350,7 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureOb
       const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
       const float wu = __fadd_rn(__fsub_rn(tmu, flu), 0.5f);
       const float wv = __fadd_rn(__fsub_rn(tmv, flv), 0.5f);
-      const float4 g = tex2Dgather<float4>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo), 0);
+      const float4 g = gather4<kMode>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo));
       const float top = fmaf(wu, g.z - g.w, g.w);
       const float bot = fmaf(wu, g.y - g.x, g.x);
       sv = fmaf(wv, bot - top, top) - sc;
@@ -335,7 +365,9 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureOb
   }
 }
 
-template <int H, bool kHw, class Ref>
+// The moments of a full window: each row's partial sums in plain FP32 (11
+// terms), the rows combined with Kahan-compensated sums.
+template <int H, int kMode, class Ref>
 __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Ref& ref,
                                                   int iu, int iv, float fu, float fv, float A0, float A1, float B0,
                                                   float B1, float c0, float c1, float rmean, float sc, float* acc) {
@@ -344,6 +376,7 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
   const float gxo = ((float)iu + 1.0f) - kM, gyo = ((float)iv + 1.0f) - kM;
   const float cuo = ((float)iu + 0.5f) + fu, cvo = ((float)iv + 0.5f) + fv;
   float ss = 0.f, sss = 0.f, srs = 0.f;
+  float cs = 0.f, css = 0.f, crs = 0.f;
 #pragma unroll 1
   for (int dy = -H; dy <= H; ++dy) {
     const float fdy = (float)dy;
@@ -351,11 +384,11 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
     float nu = fmaf(fdy, A1, -(float)H * A0);
     float nv = fmaf(fdy, B1, -(float)H * B0);
     float r_s = 0.f, r_ss = 0.f, r_rs = 0.f;
-    plane_row<H, kHw>(tex, tex_lin, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, cuo, cvo,
-                      rmean, sc, r_s, r_ss, r_rs);
-    ss += r_s;
-    sss += r_ss;
-    srs += r_rs;
+    plane_row<H, kMode>(tex, tex_lin, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, cuo,
+                        cvo, rmean, sc, r_s, r_ss, r_rs);
+    kahan_add(ss, cs, r_s);
+    kahan_add(sss, css, r_ss);
+    kahan_add(srs, crs, r_rs);
   }
   acc[2] = ss;
   acc[3] = sss;
@@ -364,7 +397,7 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
 
 // H > 0: windows of 2H+1 known at compile time, reference samples through
 // `ref` on the fast path; H == 0: any window size (runtime loop).
-template <int H, bool kHw, class Ref>
+template <int H, int kMode, class Ref>
 __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
                                                       const PlaneHyp& hp, const RefWindow& rw, const Ref& ref) {
   ViewResult bad{0.0f, 0};
@@ -421,20 +454,20 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const bool outside = front && (umax_c < ulo - 0.001f || umin_c > uhi + 0.001f || vmax_c < vlo - 0.001f ||
                                  vmin_c > vhi + 0.001f);
   // source centring value: the sample at the window centre (clamped read)
-  const float sc = kHw ? tex2D<float>(S.tex_lin, (float)iu + 0.5f + fu, (float)iv + 0.5f + fv)
-                      : bilinear(S.tex, (float)iu, (float)iv, fu, fv);
+  const float sc = kMode == kSrcTex ? tex2D<float>(S.tex_lin, (float)iu + 0.5f + fu, (float)iv + 0.5f + fv)
+                                    : bilinear<kMode>(S.tex, (float)iu, (float)iv, fu, fv);
   float acc[5], n;
   const int K = 2 * h + 1;
   const int min_valid = J.min_valid;
   if (full) {
     if constexpr (H > 0)
-      plane_window_fast<H, kHw>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
+      plane_window_fast<H, kMode>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
     else
-      plane_window<true, kHw>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+      plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
   if (outside) return bad;
-  plane_window<false, kHw>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  plane_window<false, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
 }
 

@@ -207,6 +207,9 @@ struct JobData {
   DevArray<unsigned int> filled;
   bool ran = false;
   Job J{};
+  recon_pose ref_pose{};
+  recon_camera_intrinsics ref_intr{};  // as matched (pinhole after undistortion)
+  std::vector<recon_pose> src_pose;    // per relative source k
 };
 
 // ---- plane-mode batch plans (used by the context below) ----
@@ -240,9 +243,10 @@ static std::map<TuneKey, TuneChoice>& tune_cache() {
 struct PlaneGroup {
   std::vector<JobData*> jobs;  // run order: iterations descending, then pixels descending
   int patch_half = 5;
-  bool hw = false;
+  int mode = 0;  // source read mode (kSrcExact / kSrcTex / kSrcBf16)
   int max_src = 1, max_iters = 0;
-  bool refine_any = false;
+  bool refine_any = false;  // some job refines by golden section
+  bool refine_gn = false;   // some job refines by Gauss-Newton
   long long pixels = 0;
   std::unique_ptr<PlaneBatch> pix;                    // 32 x 4 pixel tiles
   std::unique_ptr<PlaneBatch> sweep[kNumRowChoices];  // 64-column x rows sweep tiles
@@ -288,8 +292,13 @@ struct Context {
   recon_mvs_stats stats{};
 
   explicit Context(const recon_mvs_options& o) : opts(o) {
+    if (o.refine < 0 || o.refine > 2) fail(RECON_ERR_INVALID_ARGUMENT, "refine must be 0, 1 or 2");
     if (o.tile_rows != 0 && row_choice_index(o.tile_rows) < 0)
       fail(RECON_ERR_INVALID_ARGUMENT, "tile_rows must be 0 (autotuned), 2, 4 or 8");
+    if (o.storage < RECON_MVS_STORAGE_FP32 || o.storage > RECON_MVS_STORAGE_BF16)
+      fail(RECON_ERR_INVALID_ARGUMENT, "unknown storage format");
+    if (o.storage == RECON_MVS_STORAGE_BF16 && (o.mode != RECON_MVS_MODE_PLANE || o.interp != 0))
+      fail(RECON_ERR_INVALID_ARGUMENT, "BF16 storage needs plane mode with exact interpolation (interp = 0)");
     device = o.device;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -350,17 +359,23 @@ static const recon_camera_intrinsics& src_intr(const recon_mvs_views& v, int k) 
   return intrinsics_global(v) ? v.src_intrinsics[v.source_indices[k]] : v.src_intrinsics[k];
 }
 
-static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32, int w, int h, bool fp16,
+// Source texture of (I - 128) in the context's storage format: FP32, FP16
+// (both with a point-filtered gather object and a linear-filter object) or
+// BF16 bits in a 16-bit unsigned channel (gather object only).
+static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32, int w, int h, int storage,
                          Texture& T) {
-  cudaChannelFormatDesc desc = fp16 ? cudaCreateChannelDescHalf() : cudaCreateChannelDesc<float>();
+  const bool bf16 = storage == RECON_MVS_STORAGE_BF16;
+  cudaChannelFormatDesc desc = storage == RECON_MVS_STORAGE_FP16 ? cudaCreateChannelDescHalf()
+                               : bf16 ? cudaCreateChannelDesc(16, 0, 0, 0, cudaChannelFormatKindUnsigned)
+                                      : cudaCreateChannelDesc<float>();
   CK(cudaMallocArray(&T.arr, &desc, w, h, cudaArrayTextureGather));
-  const size_t elem = fp16 ? 2 : 4;
+  const size_t elem = storage == RECON_MVS_STORAGE_FP32 ? 4 : 2;
   const size_t pitch = ((size_t)w * elem + 255) & ~(size_t)255;
   C.stage_tex.alloc(pitch * h);
   if (is_f32)
-    CK(launch_prep_src_f32in((const float*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, fp16, C.stream));
+    CK(launch_prep_src_f32in((const float*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, storage, C.stream));
   else
-    CK(launch_prep_src((const uint8_t*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, fp16, C.stream));
+    CK(launch_prep_src((const uint8_t*)dev_img_u8_or_f32, w, h, C.stage_tex.p, pitch, storage, C.stream));
   CK(cudaMemcpy2DToArrayAsync(T.arr, 0, 0, C.stage_tex.p, pitch, (size_t)w * elem, h, cudaMemcpyDeviceToDevice,
                               C.stream));
   cudaResourceDesc rd;
@@ -375,8 +390,10 @@ static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32,
   td.readMode = cudaReadModeElementType;
   td.normalizedCoords = 0;
   CK(cudaCreateTextureObject(&T.tex, &rd, &td, nullptr));
-  td.filterMode = cudaFilterModeLinear;
-  CK(cudaCreateTextureObject(&T.tex_lin, &rd, &td, nullptr));
+  if (!bf16) {
+    td.filterMode = cudaFilterModeLinear;
+    CK(cudaCreateTextureObject(&T.tex_lin, &rd, &td, nullptr));
+  }
 }
 
 // Upload an 8-bit host image (optionally undistorted) to a device buffer;
@@ -426,6 +443,22 @@ static void cell_depths(const JobData& D, std::vector<double>* cell_sum, std::ve
   }
 }
 
+// The reference -> source transform of one source (composed in FP64 in the
+// reference's order) and the FP32 / float-float forms the kernels read.
+static void set_src_transform(SrcView& S, const recon_pose& ref, const recon_pose& src,
+                              const recon_camera_intrinsics& rk) {
+  double A[9], b[3];
+  relative_transform(ref, src, A, b);
+  for (int i = 0; i < 9; ++i) S.A[i] = A[i];
+  for (int i = 0; i < 3; ++i) {
+    S.bd[i] = b[i];
+    S.b[i] = (float)b[i];
+    S.bff[i] = ff_host(b[i]);
+    S.Ac0[i] = (float)(A[i * 3 + 0] / rk.fx);
+    S.Ac1[i] = (float)(A[i * 3 + 1] / rk.fy);
+  }
+}
+
 static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,
                      const double* seeds, int num_seeds) {
   validate_views(v);
@@ -440,7 +473,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   D.cfg = *cfg;
   D.opts = C.opts;
   const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
-  const bool fp16 = C.opts.storage == RECON_MVS_STORAGE_FP16;
+  const bool bf16 = C.opts.storage == RECON_MVS_STORAGE_BF16;
   recon_camera_intrinsics rk = *v->ref_intr;
   if (plane && !undistort) {
     bool any = distorted(rk);
@@ -477,7 +510,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
     DevArray<float> fl;
     const void* dev = upload_image(C, v->src_gray[k], v->src_w[k], v->src_h[k], undistort ? &sk : nullptr, u8, fl, &f32);
     auto T = std::make_unique<Texture>();
-    make_texture(C, dev, f32, v->src_w[k], v->src_h[k], fp16, *T);
+    make_texture(C, dev, f32, v->src_w[k], v->src_h[k], C.opts.storage, *T);
     CK(cudaStreamSynchronize(C.stream));  // staging buffers are reused
     if (undistort) sk.k1 = sk.k2 = sk.k3 = sk.p1 = sk.p2 = 0.0;
     SrcView& S = D.host_src[k];
@@ -500,18 +533,12 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
     S.p1 = (float)sk.p1;
     S.p2 = (float)sk.p2;
     S.distorted = distorted(sk) ? 1 : 0;
-    double A[9], b[3];
-    relative_transform(*v->ref_pose, sp, A, b);
-    for (int i = 0; i < 9; ++i) S.A[i] = A[i];
-    for (int i = 0; i < 3; ++i) {
-      S.bd[i] = b[i];
-      S.b[i] = (float)b[i];
-      S.bff[i] = ff_host(b[i]);
-      S.Ac0[i] = (float)(A[i * 3 + 0] / rk.fx);
-      S.Ac1[i] = (float)(A[i * 3 + 1] / rk.fy);
-    }
+    set_src_transform(S, *v->ref_pose, sp, rk);
+    D.src_pose.push_back(sp);
     D.tex.push_back(std::move(T));
   }
+  D.ref_pose = *v->ref_pose;
+  D.ref_intr = rk;
   D.src_table.alloc(v->num_src);
   CK(cudaMemcpyAsync(D.src_table.p, D.host_src.data(), sizeof(SrcView) * v->num_src, cudaMemcpyHostToDevice, C.stream));
 
@@ -549,7 +576,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   J.ref_de = D.ref_de.p;
   J.ref_half_w = half_w;
   J.half_pixel = (plane && C.opts.sampling == 1) ? 1 : 0;
-  J.hw_interp = (plane && C.opts.interp == 1) ? 1 : 0;
+  J.src_mode = !plane ? kSrcExact : (bf16 ? kSrcBf16 : (C.opts.interp == 1 ? kSrcTex : kSrcExact));
   J.pref = J.half_pixel ? D.ref_box.p : D.ref.p;
   J.src = D.src_table.p;
   J.dinv_min = inv_min;
@@ -607,6 +634,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
     }
     J.iterations = cfg->iterations;
     J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0) ? cfg->subpixel_iterations : 0;
+    J.refine_mode = C.opts.refine;
     J.inv_per_px = (float)D.inv_per_px;
     J.out_depth = D.out_depth.p;
     J.out_support = D.out_support.p;
@@ -653,12 +681,14 @@ static void build_group(Context& C, PlaneGroup& G) {
   G.max_src = 1;
   G.max_iters = 0;
   G.refine_any = false;
+  G.refine_gn = false;
   G.pixels = 0;
   for (int j = 0; j < n; ++j) {
     const JobData& D = *G.jobs[j];
     G.max_src = std::max(G.max_src, D.num_src);
     G.max_iters = std::max(G.max_iters, std::max(0, D.cfg.iterations));
-    G.refine_any = G.refine_any || D.J.refine_iters > 0;
+    G.refine_any = G.refine_any || (D.J.refine_iters > 0 && D.J.refine_mode == 1);
+    G.refine_gn = G.refine_gn || (D.J.refine_iters > 0 && D.J.refine_mode == 2);
     G.pixels += (long long)D.w * D.h;
     auto add = [&](PlaneBatch& B, long long tiles) {
       B.jobs[j] = D.J;
@@ -700,7 +730,7 @@ static void tune_group(Context& C, PlaneGroup& G) {
   };
   auto occupancy = [&](int rows) {
     int b = 0;
-    CK(plane_sweep_occupancy(G.patch_half, G.hw, G.max_src, rows, &b));
+    CK(plane_sweep_occupancy(G.patch_half, G.mode, G.max_src, rows, &b));
     return b;
   };
   if (C.opts.tile_rows != 0) {
@@ -709,7 +739,7 @@ static void tune_group(Context& C, PlaneGroup& G) {
     set_shape(C.opts.tile_rows, b);
     return;
   }
-  const TuneKey key{C.device, G.patch_half, G.hw ? 1 : 0, C.opts.storage, G.max_src, G.nj(), G.pixels};
+  const TuneKey key{C.device, G.patch_half, G.mode, C.opts.storage, G.max_src, G.nj(), G.pixels};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = tune_cache().find(key);
@@ -732,9 +762,9 @@ static void tune_group(Context& C, PlaneGroup& G) {
     for (int ctas = b; ctas >= std::max(1, b - 1); --ctas) {
       float ms = 0.f;
       for (int rep = 0; rep < 2; ++rep) {  // the first trial also loads the kernel
-        CK(launch_plane_init(*G.pix, G.patch_half, G.hw, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+        CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
         CK(cudaEventRecord(C.ev_sweep0, C.stream));
-        CK(launch_plane_sweep(G.sweep_batch(rows), G.sweep_total(rows, 0), G.queues.p, G.patch_half, G.hw, G.max_src,
+        CK(launch_plane_sweep(G.sweep_batch(rows), G.sweep_total(rows, 0), G.queues.p, G.patch_half, G.mode, G.max_src,
                               rows, ctas * nsm, 0, 0, C.stream));
         CK(cudaEventRecord(C.ev_sweep1, C.stream));
         CK(cudaEventSynchronize(C.ev_sweep1));
@@ -765,7 +795,7 @@ static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
   if (stage == 0) {
     for (auto& g : P.groups) {
       PlaneGroup& G = *g;
-      CK(launch_plane_init(*G.pix, G.patch_half, G.hw, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+      CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
     }
   } else if (stage == 1) {
     int launches = 0;
@@ -774,7 +804,7 @@ static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
       for (int it = 0; it < G.max_iters; ++it)
         for (int color = 0; color < 2; ++color) {
           CK(launch_plane_sweep(G.sweep_batch(G.rows), G.sweep_total(G.rows, it), G.queues.p + 2 * it + color,
-                                G.patch_half, G.hw, G.max_src, G.rows, G.grid, color, it, C.stream));
+                                G.patch_half, G.mode, G.max_src, G.rows, G.grid, color, it, C.stream));
           ++launches;
         }
     }
@@ -782,7 +812,8 @@ static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
   } else {
     for (auto& g : P.groups) {
       PlaneGroup& G = *g;
-      if (G.refine_any) CK(launch_plane_refine(*G.pix, G.patch_half, G.hw, G.max_src, C.stream));
+      if (G.refine_any) CK(launch_plane_refine(*G.pix, G.patch_half, G.mode, G.max_src, C.stream));
+      if (G.refine_gn) CK(launch_plane_refine_gn(*G.pix, G.patch_half, G.mode, G.max_src, C.stream));
       CK(launch_plane_output(*G.pix, C.stream));
     }
   }
@@ -826,12 +857,12 @@ static std::unique_ptr<PlanePlan> make_plan(Context& C, const std::vector<JobDat
     PlaneGroup* G = nullptr;
     if (!P->per_view)
       for (auto& g : P->groups)
-        if (g->patch_half == D->J.patch_half && g->hw == (D->J.hw_interp != 0) && g->nj() < kBatchJobs) G = g.get();
+        if (g->patch_half == D->J.patch_half && g->mode == D->J.src_mode && g->nj() < kBatchJobs) G = g.get();
     if (!G) {
       P->groups.push_back(std::make_unique<PlaneGroup>());
       G = P->groups.back().get();
       G->patch_half = D->J.patch_half;
-      G->hw = D->J.hw_interp != 0;
+      G->mode = D->J.src_mode;
     }
     G->jobs.push_back(D);
   }
@@ -1332,6 +1363,241 @@ RECON_API recon_status recon_mvs_evaluate(const recon_mvs_views* views, const re
     if (out_view_cost)
       CK(cudaMemcpyAsync(out_view_cost, dv.p, (size_t)n * D.num_src * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
     CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+// ---- the differentiation form ---------------------------------------------
+static void check_hyps(const JobData& D, int n, const int32_t* px, const int32_t* py, const double* depth,
+                       const double* angles) {
+  if (n < 0 || (n > 0 && (!px || !py || !depth || !angles))) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (D.opts.mode != RECON_MVS_MODE_PLANE) fail(RECON_ERR_INVALID_ARGUMENT, "the adjoint needs a plane-mode job");
+  if (D.num_src > kMaxSources) fail(RECON_ERR_INVALID_ARGUMENT, "more than 32 sources");
+  for (int i = 0; i < n; ++i)
+    if (px[i] < 0 || py[i] < 0 || px[i] >= D.w || py[i] >= D.h) fail(RECON_ERR_INVALID_ARGUMENT, "pixel outside image");
+}
+
+struct HypUpload {
+  DevArray<int> x, y;
+  DevArray<double> d, a;
+  void put(Context& C, int n, const int32_t* px, const int32_t* py, const double* depth, const double* angles) {
+    x.alloc(n);
+    y.alloc(n);
+    d.alloc(n);
+    a.alloc((size_t)2 * n);
+    CK(cudaMemcpyAsync(x.p, px, n * sizeof(int), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(y.p, py, n * sizeof(int), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(d.p, depth, n * sizeof(double), cudaMemcpyHostToDevice, C.stream));
+    CK(cudaMemcpyAsync(a.p, angles, (size_t)2 * n * sizeof(double), cudaMemcpyHostToDevice, C.stream));
+  }
+};
+
+RECON_API recon_status recon_mvs_job_adjoint(void* ctx, int32_t job, int32_t n, const int32_t* px, const int32_t* py,
+                                             const double* depth, const double* angles, float* out_cost,
+                                             float* out_grad, float* out_gn, float* out_pose_grad) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    JobData& D = get_job(C, job);
+    check_hyps(D, n, px, py, depth, angles);
+    if (n > 0 && (!out_cost || !out_grad)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL output");
+    if (n == 0) return;
+    HypUpload U;
+    U.put(C, n, px, py, depth, angles);
+    DevArray<float> dc, dg, dh, dp;
+    dc.alloc(n);
+    dg.alloc((size_t)3 * n);
+    if (out_gn) dh.alloc((size_t)6 * n);
+    if (out_pose_grad) dp.alloc((size_t)6 * n * D.num_src);
+    CK(launch_plane_adjoint(D.J, n, U.x.p, U.y.p, U.d.p, U.a.p, dc.p, dg.p, out_gn ? dh.p : nullptr,
+                            out_pose_grad ? dp.p : nullptr, C.stream));
+    CK(cudaMemcpyAsync(out_cost, dc.p, n * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaMemcpyAsync(out_grad, dg.p, (size_t)3 * n * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    if (out_gn) CK(cudaMemcpyAsync(out_gn, dh.p, (size_t)6 * n * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+    if (out_pose_grad)
+      CK(cudaMemcpyAsync(out_pose_grad, dp.p, (size_t)6 * n * D.num_src * sizeof(float), cudaMemcpyDeviceToHost,
+                         C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
+// Rodrigues: R = exp([w]x), FP64.
+static void so3_exp(const double w[3], double R[9]) {
+  const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  const double K[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+  double a, b;
+  if (th < 1e-12) {
+    a = 1.0;
+    b = 0.5;
+  } else {
+    a = std::sin(th) / th;
+    b = (1.0 - std::cos(th)) / (th * th);
+  }
+  double K2[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double t = 0.0;
+      for (int q = 0; q < 3; ++q) t += K[i * 3 + q] * K[q * 3 + j];
+      K2[i * 3 + j] = t;
+    }
+  for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0 ? 1.0 : 0.0) + a * K[i] + b * K2[i];
+}
+
+// Left perturbation of a world -> camera pose in the camera frame:
+// R' = exp([w]x) R, t' = exp([w]x) t + tau.
+static recon_pose perturb_pose(const recon_pose& p, const double w[3], const double tau[3]) {
+  double E[9];
+  so3_exp(w, E);
+  recon_pose q = p;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) {
+      double t = 0.0;
+      for (int k = 0; k < 3; ++k) t += E[i * 3 + k] * p.r[k * 3 + j];
+      q.r[i * 3 + j] = t;
+    }
+    double t = 0.0;
+    for (int k = 0; k < 3; ++k) t += E[i * 3 + k] * p.t[k];
+    q.t[i] = t + tau[i];
+  }
+  return q;
+}
+
+// Solves (H + lambda diag(H)) x = -g for symmetric positive 6 x 6 H given as
+// its upper triangle (row-major order), by Cholesky in FP64.
+static bool solve_lm6(const double* Hu, const double* g, double lambda, double x[6]) {
+  double M[36];
+  int t = 0;
+  for (int i = 0; i < 6; ++i)
+    for (int j = i; j < 6; ++j, ++t) M[i * 6 + j] = M[j * 6 + i] = Hu[t];
+  for (int i = 0; i < 6; ++i) M[i * 6 + i] *= 1.0 + lambda;
+  double L[36] = {0};
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double s = M[i * 6 + j];
+      for (int k = 0; k < j; ++k) s -= L[i * 6 + k] * L[j * 6 + k];
+      if (i == j) {
+        if (!(s > 0.0)) return false;
+        L[i * 6 + i] = std::sqrt(s);
+      } else {
+        L[i * 6 + j] = s / L[j * 6 + j];
+      }
+    }
+  double y[6];
+  for (int i = 0; i < 6; ++i) {
+    double s = -g[i];
+    for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
+    y[i] = s / L[i * 6 + i];
+  }
+  for (int i = 5; i >= 0; --i) {
+    double s = y[i];
+    for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * x[k];
+    x[i] = s / L[i * 6 + i];
+  }
+  for (int i = 0; i < 6; ++i)
+    if (!std::isfinite(x[i])) return false;
+  return true;
+}
+
+// Per-source sums of the pose normal equations over the hypotheses.
+struct PoseSums {
+  std::vector<double> cost, count, g, H;  // per source: 1, 1, 6, 21
+};
+
+static PoseSums pose_normal_eq(Context& C, JobData& D, const HypUpload& U, int n, DevArray<float>& part) {
+  const int rec = pose_partial_records();
+  const int blocks = (n + 127) / 128;
+  const int S = D.num_src;
+  part.alloc((size_t)blocks * S * rec);
+  CK(launch_pose_normal_eq(D.J, n, U.x.p, U.y.p, U.d.p, U.a.p, part.p, C.stream));
+  std::vector<float> host((size_t)blocks * S * rec);
+  CK(cudaMemcpyAsync(host.data(), part.p, host.size() * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  PoseSums P;
+  P.cost.assign(S, 0.0);
+  P.count.assign(S, 0.0);
+  P.g.assign((size_t)S * 6, 0.0);
+  P.H.assign((size_t)S * 21, 0.0);
+  for (int b = 0; b < blocks; ++b)
+    for (int s = 0; s < S; ++s) {
+      const float* r = &host[((size_t)b * S + s) * rec];
+      P.cost[s] += r[0];
+      for (int i = 0; i < 6; ++i) P.g[(size_t)s * 6 + i] += r[1 + i];
+      for (int i = 0; i < 21; ++i) P.H[(size_t)s * 21 + i] += r[7 + i];
+      P.count[s] += r[28];
+    }
+  return P;
+}
+
+static void upload_src_table(Context& C, JobData& D) {
+  CK(cudaMemcpyAsync(D.src_table.p, D.host_src.data(), sizeof(SrcView) * D.num_src, cudaMemcpyHostToDevice,
+                     C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+}
+
+RECON_API recon_status recon_mvs_job_recover_poses(void* ctx, int32_t job, int32_t n, const int32_t* px,
+                                                   const int32_t* py, const double* depth, const double* angles,
+                                                   int32_t iterations, recon_pose* out_src_poses,
+                                                   double* out_cost) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    if (iterations < 0) fail(RECON_ERR_INVALID_ARGUMENT, "iterations < 0");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    JobData& D = get_job(C, job);
+    check_hyps(D, n, px, py, depth, angles);
+    if (D.degenerate) fail(RECON_ERR_INVALID_ARGUMENT, "degenerate job");
+    if (C.plan && std::find(C.plan->ids.begin(), C.plan->ids.end(), job) != C.plan->ids.end()) {
+      CK(cudaStreamSynchronize(C.stream));
+      C.plan.reset();  // the captured launches carry the job's old transforms
+    }
+    const int S = D.num_src;
+    HypUpload U;
+    U.put(C, n, px, py, depth, angles);
+    DevArray<float> part;
+    auto mean = [](const PoseSums& P, int s) { return P.count[s] > 0 ? P.cost[s] / P.count[s] : 1e30; };
+    PoseSums cur = pose_normal_eq(C, D, U, n, part);
+    auto total = [&](const PoseSums& P) {
+      double t = 0.0;
+      for (int s = 0; s < S; ++s) t += mean(P, s);
+      return t;
+    };
+    if (out_cost) out_cost[0] = total(cur);
+    std::vector<double> lambda(S, 1e-4);
+    for (int it = 0; it < iterations; ++it) {
+      std::vector<recon_pose> prev = D.src_pose;
+      std::vector<bool> moved(S, false);
+      for (int s = 0; s < S; ++s) {
+        if (cur.count[s] < 6) continue;
+        double x[6];
+        if (!solve_lm6(&cur.H[(size_t)s * 21], &cur.g[(size_t)s * 6], lambda[s], x)) {
+          lambda[s] *= 10.0;
+          continue;
+        }
+        D.src_pose[s] = perturb_pose(prev[s], x, x + 3);
+        set_src_transform(D.host_src[s], D.ref_pose, D.src_pose[s], D.ref_intr);
+        moved[s] = true;
+      }
+      upload_src_table(C, D);
+      PoseSums trial = pose_normal_eq(C, D, U, n, part);
+      for (int s = 0; s < S; ++s) {
+        if (!moved[s]) continue;
+        if (mean(trial, s) < mean(cur, s)) {
+          cur.cost[s] = trial.cost[s];
+          cur.count[s] = trial.count[s];
+          for (int i = 0; i < 6; ++i) cur.g[(size_t)s * 6 + i] = trial.g[(size_t)s * 6 + i];
+          for (int i = 0; i < 21; ++i) cur.H[(size_t)s * 21 + i] = trial.H[(size_t)s * 21 + i];
+          lambda[s] *= 0.3;
+        } else {
+          D.src_pose[s] = prev[s];
+          set_src_transform(D.host_src[s], D.ref_pose, D.src_pose[s], D.ref_intr);
+          lambda[s] *= 10.0;
+        }
+      }
+      upload_src_table(C, D);
+      if (out_cost) out_cost[it + 1] = total(cur);
+    }
+    if (out_src_poses)
+      for (int s = 0; s < S; ++s) out_src_poses[s] = D.src_pose[s];
   });
 }
 

@@ -66,13 +66,27 @@ struct PlaneBatch {
   int njobs;
 };
 static_assert(sizeof(PlaneBatch) + 64 <= 32764, "PlaneBatch exceeds the kernel-parameter limit");
-cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, bool hw, int max_src, int* queues, int num_queues,
+cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int max_src, int* queues, int num_queues,
                               cudaStream_t st);
-cudaError_t plane_sweep_occupancy(int patch_half, bool hw, int max_src, int rows, int* blocks_per_sm);
-cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, bool hw, int max_src,
+cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int* blocks_per_sm);
+cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, int mode, int max_src,
                                int rows, int grid, int color, int iter, cudaStream_t st);
-cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, bool hw, int max_src, cudaStream_t st);
+cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st);
+cudaError_t launch_plane_refine_gn(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st);
 cudaError_t launch_plane_output(const PlaneBatch& B, cudaStream_t st);
+
+// ---- the differentiation form (adjoint.cu) ----
+// Per hypothesis (pixel, depth, theta / phi): cost, gradient (d, theta, phi),
+// Gauss-Newton matrix (6, upper triangle; optional), pose gradient
+// (num_src x 6: rotation, translation; optional).
+cudaError_t launch_plane_adjoint(const Job& J, int n, const int* px, const int* py, const double* depth,
+                                 const double* angles, float* cost, float* grad, float* gn, float* pose_grad,
+                                 cudaStream_t st);
+// Pose normal equations: per (block, source) records of pose_partial_records()
+// floats: cost sum, gradient (6), Gauss-Newton matrix (21), pixel count.
+int pose_partial_records();
+cudaError_t launch_pose_normal_eq(const Job& J, int n, const int* px, const int* py, const double* depth,
+                                  const double* angles, float* partial, cudaStream_t st);
 
 cudaError_t launch_compat_init(const Job& J, float* cost, cudaStream_t st);
 cudaError_t launch_compat_sweep(const Job& J, const double* inv_in, const float* cost_in, const int32_t* sup_in,
@@ -85,9 +99,9 @@ cudaError_t launch_compat_refine(const Job& J, float* depth, float* conf, double
                                  unsigned int* refined, double* best_inv, float* best_cost, cudaStream_t st);
 cudaError_t launch_prep_ref(const uint8_t* img, int w, int h, float* ref, float* box, cudaStream_t st);
 cudaError_t launch_prep_ref_f32(const float* img, int w, int h, float* ref, float* box, cudaStream_t st);
-cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                             cudaStream_t st);
-cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                                   cudaStream_t st);
 cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, float* out, cudaStream_t st);
 cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);

@@ -12,11 +12,13 @@
 // reference's Jacobi sweeps (every pixel reads the sweep's snapshot,
 // patchmatch_stereo.cpp:615-740), run one thread per pixel; the reference's
 // row-block xorshift draws are generated on the host in its scan order.
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cstdio>
 #include <type_traits>
 
+#include "adjoint.cuh"
 #include "cost.cuh"
 #include "kernels.h"
 
@@ -62,8 +64,6 @@ struct HypCost {
   int support;
 };
 
-constexpr int kMaxBestK = 8;
-
 __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int nvalid, int best_k,
                                                 float photo_threshold) {
   HypCost r{kCostInf, nvalid};
@@ -83,7 +83,7 @@ __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int 
   return r;
 }
 
-template <int H, bool kHw, class Ref>
+template <int H, int kMode, class Ref>
 __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
                                   float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
                                   int* nevals = nullptr) {
@@ -100,7 +100,7 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
   for (int s = 0; s < J.num_src; ++s) {
     ff P[3];
     pc.get(s, P);
-    const ViewResult v = eval_view_plane<H, kHw>(J, J.src[s], x, y, P, hp, rw, ref);
+    const ViewResult v = eval_view_plane<H, kMode>(J, J.src[s], x, y, P, hp, rw, ref);
     float c = kCostInf;
     if (v.valid) {
       c = 1.0f - v.ncc;
@@ -151,7 +151,7 @@ __device__ HypCost eval_compat_hyp(const Job& J, const PCache& pc, int x, int y,
 // ---------------------------------------------------------------------------
 // batch evaluation of given hypotheses (parity instrument, adjoint driver)
 // ---------------------------------------------------------------------------
-template <int H, bool kHw>
+template <int H, int kMode>
 __global__ void __launch_bounds__(128, 4) k_eval_hyps(Job J, int mode, int n, const int* __restrict__ px, const int* __restrict__ py,
                             const double* __restrict__ inv, const float* __restrict__ normals, float* out_cost,
                             int* out_support, float* out_view_cost) {
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(128, 4) k_eval_hyps(Job J, int mode, int n, co
   } else {
     const RefWindow rw = ref_window(J, x, y, J.half_pixel);
     const GlobalRef ref{J.pref, J.w, x, y};
-    r = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
+    r = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, (float)inv[i], normals[3 * i], normals[3 * i + 1], normals[3 * i + 2],
                           rw, ref, vc);
   }
   out_cost[i] = r.cost;
@@ -269,7 +269,7 @@ __device__ __forceinline__ bool pixel_item(const PlaneBatch& B, int* job, int* x
 // Random initialisation (and seed cells) + initial cost.  Block 0 also zeroes
 // the work counters of the persistent sweeps that follow, and each job's
 // first pixel zeroes its filled counter.
-template <int H, bool kHw>
+template <int H, int kMode>
 __global__ void __launch_bounds__(128, 4) k_plane_init(const __grid_constant__ PlaneBatch B, int* queues,
                                                        int num_queues) {
   extern __shared__ float2 smem[];
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128, 4) k_plane_init(const __grid_constant__ P
   }
   const RefWindow rw = ref_window(J, x, y, J.half_pixel);
   const GlobalRef ref{J.pref, J.w, x, y};
-  const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
+  const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr);
   J.hyp[idx] = make_float4(rho, nx, ny, nz);
   J.cost[idx] = c.cost;
   J.support[idx] = (uint8_t)min(c.support, 255);
@@ -356,7 +356,7 @@ __device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t,
 
 // One red-black half-sweep of one pixel: propagation from the best-cost
 // neighbour of each of the 8 adaptive regions, then 5 refinement hypotheses.
-template <int H, bool kHw, class RefT>
+template <int H, int kMode, class RefT>
 __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, const RefT& ref, const RefWindow& rw,
                                             int x, int y, int color, int iter) {
   const int idx = y * J.w + x;
@@ -404,7 +404,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
     if (!(rho > 0.f)) continue;
     if (rho == cur.x && hn.y == cur.y && hn.z == cur.z && hn.w == cur.w) continue;
-    const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);
@@ -431,7 +431,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
     }
-    const HypCost c = eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, nx, ny, nz);
@@ -457,7 +457,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
 // (zeroed by the init kernel); `total` its item count -- jobs with fewer
 // iterations than `iter + 1` sit at the end of the job order and fall
 // outside it.
-template <int H, bool kHw>
+template <int H, int kMode>
 __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch B, int total, int* queue, int color,
                                               int iter) {
   extern __shared__ float2 smem[];
@@ -500,11 +500,11 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
         const TileRef ref{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
                           (int)threadIdx.x, parity, (int)threadIdx.y};
         const RefWindow rw = tile_window<H>(J, ref, x, y);
-        sweep_pixel<H, kHw>(J, pc, ref, rw, x, y, color, iter);
+        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
       } else {
         const GlobalRef ref{J.pref, J.w, x, y};
         const RefWindow rw = ref_window(J, x, y, J.half_pixel);
-        sweep_pixel<H, kHw>(J, pc, ref, rw, x, y, color, iter);
+        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
       }
     }
     __syncthreads();
@@ -810,14 +810,14 @@ __global__ void k_compat_refine(Job J, float* depth, float* conf, double inv_per
 // Plane-mode refinement: golden-section search on the inverse depth along
 // the pixel's own plane normal over +-1 px of disparity, the reference's
 // refinement schedule applied to the plane cost.
-template <int H, bool kHw>
+template <int H, int kMode>
 __global__ void __launch_bounds__(128, 4) k_plane_refine(const __grid_constant__ PlaneBatch B) {
   extern __shared__ float2 smem[];
   const int tid = threadIdx.y * 32 + threadIdx.x;
   int j, x, y;
   if (!pixel_item(B, &j, &x, &y)) return;
   const Job& J = B.jobs[j];
-  if (J.refine_iters <= 0) return;
+  if (J.refine_iters <= 0 || J.refine_mode != 1) return;
   PCache pc{smem, 128, tid};
   const int idx = y * J.w + x;
   const float4 h0 = J.hyp[idx];
@@ -828,7 +828,7 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine(const __grid_constant__
   const RefWindow rw = ref_window(J, x, y, J.half_pixel);
   const GlobalRef ref{J.pref, J.w, x, y};
   auto eval = [&](float v) -> HypCost {
-    return eval_plane_hyp<H, kHw>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
+    return eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, v, h0.y, h0.z, h0.w, rw, ref, nullptr);
   };
   float best_d = h0.x, best_c = c0;
   int best_s = J.support[idx];
@@ -876,6 +876,68 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine(const __grid_constant__
   J.support[idx] = (uint8_t)min(best_s, 255);
 }
 
+// Plane-mode Gauss-Newton refinement (refine mode 2): Levenberg-Marquardt
+// steps on (d, theta, phi) from the adjoint of the aggregated cost (exact
+// bilinear reads, window recomputed per pass), each step accepted only when
+// the search's own cost of the new plane is lower.
+template <int H, int kMode>
+__global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constant__ PlaneBatch B) {
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  int j, x, y;
+  if (!pixel_item(B, &j, &x, &y)) return;
+  const Job& J = B.jobs[j];
+  if (J.refine_iters <= 0 || J.refine_mode != 2) return;
+  PCache pc{smem, 128, tid};
+  const int idx = y * J.w + x;
+  const float4 h0 = J.hyp[idx];
+  float cur = J.cost[idx];
+  if (!(cur < 1e29f) || !(h0.x > 0.f)) return;
+  int sup = J.support[idx];
+  float rx, ry;
+  fill_pcache(J, pc, x, y, &rx, &ry);
+  const RefWindow rw = ref_window(J, x, y, J.half_pixel);
+  const GlobalRef ref{J.pref, J.w, x, y};
+  float d = 1.0f / h0.x;
+  float theta = acosf(fminf(1.0f, fmaxf(-1.0f, h0.w))), phi = atan2f(h0.z, h0.y);
+  float4 best = h0;
+  float lambda = 1e-3f;
+  for (int it = 0; it < J.refine_iters; ++it) {
+    AdjHyp ah;
+    if (!make_adj_hyp(J, x, y, d, theta, phi, &ah)) break;
+    float c, g[3], Hm[6];
+    if (plane_adjoint<kMode>(J, ah, &c, g, Hm, nullptr) == 0) break;
+    bool accepted = false;
+    for (int t = 0; t < 4 && !accepted; ++t) {
+      float step[3];
+      if (!solve_lm3(Hm, g, lambda, step)) {
+        lambda *= 10.0f;
+        continue;
+      }
+      const float nd = d + step[0], nt = theta + step[1], np = phi + step[2];
+      float n[3], dt[3], dp[3];
+      sph_normal(nt, np, n, dt, dp);
+      const HypCost hc = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, 1.0f / nd, n[0], n[1], n[2], rw, ref, nullptr);
+      if (nd > 0.f && hc.cost < cur) {
+        d = nd;
+        theta = nt;
+        phi = np;
+        cur = hc.cost;
+        sup = hc.support;
+        best = make_float4(1.0f / nd, n[0], n[1], n[2]);
+        lambda *= 0.3f;
+        accepted = true;
+      } else {
+        lambda *= 10.0f;
+      }
+    }
+    if (!accepted) break;
+  }
+  J.hyp[idx] = best;
+  J.cost[idx] = cur;
+  J.support[idx] = (uint8_t)min(sup, 255);
+}
+
 // ---------------------------------------------------------------------------
 // image preparation
 // ---------------------------------------------------------------------------
@@ -906,18 +968,23 @@ __global__ void k_deinterleave(const float* __restrict__ ref, int w, int h, int 
   }
 }
 
-__global__ void k_prep_src_f32(const uint8_t* __restrict__ img, int w, int h, float* out, size_t pitch_elems) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= w || y >= h) return;
-  out[y * pitch_elems + x] = (float)img[y * w + x] - 128.0f;
+// One staged source texel of (I - 128) in the storage format (0 FP32, 1 FP16,
+// 2 BF16 bits), rounded to nearest even.
+__device__ __forceinline__ void store_texel(void* out, size_t i, float v, int storage) {
+  if (storage == 1)
+    ((__half*)out)[i] = __float2half_rn(v);
+  else if (storage == 2)
+    ((unsigned short*)out)[i] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  else
+    ((float*)out)[i] = v;
 }
 
-__global__ void k_prep_src_f16(const uint8_t* __restrict__ img, int w, int h, __half* out, size_t pitch_elems) {
+__global__ void k_prep_src(const uint8_t* __restrict__ img, int w, int h, void* out, size_t pitch_elems,
+                           int storage) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= w || y >= h) return;
-  out[y * pitch_elems + x] = __float2half_rn((float)img[y * w + x] - 128.0f);
+  store_texel(out, y * pitch_elems + x, (float)img[y * w + x] - 128.0f, storage);
 }
 
 __global__ void k_prep_ref_f32(const float* __restrict__ img, int w, int h, float* ref, float* box) {
@@ -932,15 +999,12 @@ __global__ void k_prep_ref_f32(const float* __restrict__ img, int w, int h, floa
   }
 }
 
-__global__ void k_prep_src_f32in(const float* __restrict__ img, int w, int h, void* out, size_t pitch_elems, int fp16) {
+__global__ void k_prep_src_f32in(const float* __restrict__ img, int w, int h, void* out, size_t pitch_elems,
+                                 int storage) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= w || y >= h) return;
-  const float v = img[y * w + x] - 128.0f;
-  if (fp16)
-    ((__half*)out)[y * pitch_elems + x] = __float2half_rn(v);
-  else
-    ((float*)out)[y * pitch_elems + x] = v;
+  store_texel(out, y * pitch_elems + x, img[y * w + x] - 128.0f, storage);
 }
 
 // ComputeNcc (patchmatch_stereo.cpp:214-274) for a batch of windows, FP64 in
@@ -1010,45 +1074,7 @@ __global__ void k_gather_probe(cudaTextureObject_t tex, float x, float y, float4
 // ---------------------------------------------------------------------------
 static size_t pcache_bytes(int num_src, int threads) { return (size_t)num_src * 3 * threads * sizeof(float2); }
 
-cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const int* py, const double* inv,
-                             const float* normals, float* cost, int* support, float* view_cost, cudaStream_t st) {
-  const int threads = 128;
-  const int blocks = (n + threads - 1) / threads;
-  if (blocks == 0) return cudaSuccess;
-  const size_t sm = pcache_bytes(J.num_src, threads);
-  if (J.hw_interp) {
-    if (J.patch_half == 5)
-      k_eval_hyps<5, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-    else if (J.patch_half == 3)
-      k_eval_hyps<3, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-    else
-      k_eval_hyps<0, true><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-  } else {
-    if (J.patch_half == 5)
-      k_eval_hyps<5, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-    else if (J.patch_half == 3)
-      k_eval_hyps<3, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-    else
-      k_eval_hyps<0, false><<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
-  }
-  return cudaGetLastError();
-}
-
 static dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
-
-// Calls f(integral_constant<H>, bool_constant<kHw>) for the compiled window
-// sizes (11x11, 7x7, and the generic runtime-size path).
-template <class F>
-static cudaError_t dispatch_plane(int patch_half, bool hw, F&& f) {
-  if (hw) {
-    if (patch_half == 5) return f(std::integral_constant<int, 5>{}, std::true_type{});
-    if (patch_half == 3) return f(std::integral_constant<int, 3>{}, std::true_type{});
-    return f(std::integral_constant<int, 0>{}, std::true_type{});
-  }
-  if (patch_half == 5) return f(std::integral_constant<int, 5>{}, std::false_type{});
-  if (patch_half == 3) return f(std::integral_constant<int, 3>{}, std::false_type{});
-  return f(std::integral_constant<int, 0>{}, std::false_type{});
-}
 
 // Dynamic shared memory above the 48 KB default needs an opt-in per kernel.
 template <class K>
@@ -1057,12 +1083,47 @@ static cudaError_t allow_smem(K* kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, bool hw, int max_src, int* queues, int num_queues,
+// Calls f(integral_constant<H>, integral_constant<kMode>) for the compiled
+// window sizes (11x11, 7x7, and the generic runtime-size path) and source
+// modes; BF16 sources have the 11x11 and generic instances only.
+template <class F>
+static cudaError_t dispatch_plane(int patch_half, int mode, F&& f) {
+  using std::integral_constant;
+  if (mode == kSrcTex) {
+    if (patch_half == 5) return f(integral_constant<int, 5>{}, integral_constant<int, kSrcTex>{});
+    if (patch_half == 3) return f(integral_constant<int, 3>{}, integral_constant<int, kSrcTex>{});
+    return f(integral_constant<int, 0>{}, integral_constant<int, kSrcTex>{});
+  }
+  if (mode == kSrcBf16) {
+    if (patch_half == 5) return f(integral_constant<int, 5>{}, integral_constant<int, kSrcBf16>{});
+    return f(integral_constant<int, 0>{}, integral_constant<int, kSrcBf16>{});
+  }
+  if (patch_half == 5) return f(integral_constant<int, 5>{}, integral_constant<int, kSrcExact>{});
+  if (patch_half == 3) return f(integral_constant<int, 3>{}, integral_constant<int, kSrcExact>{});
+  return f(integral_constant<int, 0>{}, integral_constant<int, kSrcExact>{});
+}
+
+cudaError_t launch_eval_hyps(const Job& J, int mode, int n, const int* px, const int* py, const double* inv,
+                             const float* normals, float* cost, int* support, float* view_cost, cudaStream_t st) {
+  const int threads = 128;
+  const int blocks = (n + threads - 1) / threads;
+  if (blocks == 0) return cudaSuccess;
+  const size_t sm = pcache_bytes(J.num_src, threads);
+  return dispatch_plane(J.patch_half, J.src_mode, [&](auto h, auto k) {
+    auto* fn = k_eval_hyps<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    fn<<<blocks, threads, sm, st>>>(J, mode, n, px, py, inv, normals, cost, support, view_cost);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int max_src, int* queues, int num_queues,
                               cudaStream_t st) {
   const int total = B.start[B.njobs];
   if (total <= 0) return cudaSuccess;
   const size_t sm = pcache_bytes(max_src, 128);
-  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
     auto* fn = k_plane_init<decltype(h)::value, decltype(k)::value>;
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
@@ -1071,9 +1132,9 @@ cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, bool hw, int 
   });
 }
 
-cudaError_t plane_sweep_occupancy(int patch_half, bool hw, int max_src, int rows, int* blocks_per_sm) {
+cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int* blocks_per_sm) {
   const size_t sm = pcache_bytes(max_src, 32 * rows);
-  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
     auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
@@ -1081,12 +1142,12 @@ cudaError_t plane_sweep_occupancy(int patch_half, bool hw, int max_src, int rows
   });
 }
 
-cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, bool hw, int max_src,
+cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, int mode, int max_src,
                                int rows, int grid, int color, int iter, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   if (rows < 1 || rows > kMaxTileRows || grid < 1 || total > B.start[B.njobs]) return cudaErrorInvalidValue;
   const size_t sm = pcache_bytes(max_src, 32 * rows);
-  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
     auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
@@ -1095,12 +1156,25 @@ cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int p
   });
 }
 
-cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, bool hw, int max_src, cudaStream_t st) {
+cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st) {
   const int total = B.start[B.njobs];
   if (total <= 0) return cudaSuccess;
   const size_t sm = pcache_bytes(max_src, 128);
-  return dispatch_plane(patch_half, hw, [&](auto h, auto k) {
+  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
     auto* fn = k_plane_refine<decltype(h)::value, decltype(k)::value>;
+    cudaError_t e = allow_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    fn<<<total, dim3(32, 4), sm, st>>>(B);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_plane_refine_gn(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st) {
+  const int total = B.start[B.njobs];
+  if (total <= 0) return cudaSuccess;
+  const size_t sm = pcache_bytes(max_src, 128);
+  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
+    auto* fn = k_plane_refine_gn<decltype(h)::value, decltype(k)::value>;
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
     fn<<<total, dim3(32, 4), sm, st>>>(B);
@@ -1154,13 +1228,10 @@ cudaError_t launch_prep_ref(const uint8_t* img, int w, int h, float* ref, float*
   return cudaGetLastError();
 }
 
-cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                             cudaStream_t st) {
   const dim3 b(32, 8);
-  if (fp16)
-    k_prep_src_f16<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, (__half*)out, pitch_bytes / sizeof(__half));
-  else
-    k_prep_src_f32<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, (float*)out, pitch_bytes / sizeof(float));
+  k_prep_src<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (storage == 0 ? 4 : 2), storage);
   return cudaGetLastError();
 }
 
@@ -1170,10 +1241,10 @@ cudaError_t launch_prep_ref_f32(const float* img, int w, int h, float* ref, floa
   return cudaGetLastError();
 }
 
-cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int fp16,
+cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                                   cudaStream_t st) {
   const dim3 b(32, 8);
-  k_prep_src_f32in<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (fp16 ? 2 : 4), fp16);
+  k_prep_src_f32in<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (storage == 0 ? 4 : 2), storage);
   return cudaGetLastError();
 }
 

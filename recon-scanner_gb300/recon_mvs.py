@@ -30,6 +30,7 @@ MODE_COMPAT = 0
 MODE_PLANE = 1
 STORAGE_FP32 = 0
 STORAGE_FP16 = 1
+STORAGE_BF16 = 2
 
 
 class Intrinsics(C.Structure):
@@ -173,6 +174,13 @@ _SIGS = {
     "recon_mvs_job_run": (C.c_int, [C.c_void_p, C.c_int32]),
     "recon_mvs_jobs_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
     "recon_mvs_job_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(DepthMapC), C.POINTER(C.c_uint32)]),
+    "recon_mvs_job_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float)]),
+    "recon_mvs_job_recover_poses": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                              C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.c_int32, C.POINTER(Pose), C.POINTER(C.c_double)]),
     "recon_mvs_job_release": (C.c_int, [C.c_void_p, C.c_int32]),
     "recon_mvs_synchronize": (C.c_int, [C.c_void_p]),
     "recon_mvs_context_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
@@ -451,12 +459,14 @@ class Engine:
         self.ctx = C.c_void_p()
         _check(_lib().recon_mvs_context_create(C.byref(self.options), C.byref(self.ctx)))
         self._keep = {}
+        self._nsrc = {}
 
     def stage(self, views: ViewArgs, config: MvsConfig, undistort=False) -> int:
         job = C.c_int32()
         _check(_lib().recon_mvs_job_stage(self.ctx, C.byref(views.struct), C.byref(config), int(undistort),
                                           C.byref(job)))
         self._keep[job.value] = views.shape
+        self._nsrc[job.value] = len(views.srcs)
         return job.value
 
     def run(self, job: int):
@@ -474,6 +484,42 @@ class Engine:
         _check(_lib().recon_mvs_job_download(self.ctx, job, C.byref(st), C.byref(f)))
         dm.filled = int(f.value)
         return dm
+
+    def adjoint(self, job: int, px, py, depth, angles, gn=False, pose=False):
+        """The adjoint at hypotheses (pixel, depth, theta/phi).  Returns
+        (cost n, grad n x 3, gn n x 6 or None, pose_grad n x S x 6 or None)."""
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        depth = np.ascontiguousarray(depth, np.float64)
+        angles = np.ascontiguousarray(angles, np.float64).reshape(-1, 2)
+        n = len(px)
+        cost = np.zeros(n, np.float32)
+        grad = np.zeros((n, 3), np.float32)
+        H = np.zeros((n, 6), np.float32) if gn else None
+        ns = self._nsrc[job]
+        pg = np.zeros((n, ns, 6), np.float32) if pose else None
+        _check(_lib().recon_mvs_job_adjoint(self.ctx, job, n, _ptr(px, C.c_int32), _ptr(py, C.c_int32),
+                                            _ptr(depth, C.c_double), _ptr(angles, C.c_double),
+                                            _ptr(cost, C.c_float), _ptr(grad, C.c_float),
+                                            _ptr(H, C.c_float) if gn else None,
+                                            _ptr(pg, C.c_float) if pose else None))
+        return cost, grad, H, pg
+
+    def recover_poses(self, job: int, px, py, depth, angles, iterations=10):
+        """Pose recovery on the job's sources.  Returns (poses num_src x 12
+        [R row-major, t], cost history)."""
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        depth = np.ascontiguousarray(depth, np.float64)
+        angles = np.ascontiguousarray(angles, np.float64).reshape(-1, 2)
+        ns = self._nsrc[job]
+        poses = (Pose * ns)()
+        hist = np.zeros(iterations + 1, np.float64)
+        _check(_lib().recon_mvs_job_recover_poses(self.ctx, job, len(px), _ptr(px, C.c_int32), _ptr(py, C.c_int32),
+                                                  _ptr(depth, C.c_double), _ptr(angles, C.c_double), iterations,
+                                                  poses, _ptr(hist, C.c_double)))
+        out = np.array([[*p.r, *p.t] for p in poses], np.float64)
+        return out, hist
 
     def release(self, job: int):
         _check(_lib().recon_mvs_job_release(self.ctx, job))
