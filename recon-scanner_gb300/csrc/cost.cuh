@@ -365,6 +365,70 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureOb
   }
 }
 
+// The moments of a window that straddles a source border (reference part
+// inside the image, plane facing the camera): each sample carries a validity
+// mask -- its source position inside [0, w-1] x [0, h-1] -- and the reference
+// moments are accumulated too.  Plane-side and denominator signs need no
+// per-sample test: they are affine in (dx, dy) and the corner test found them
+// right at all four corners.  Rows are combined with Kahan-compensated sums.
+template <int H, int kMode, class Ref>
+__device__ __forceinline__ void plane_window_masked(const SrcView& S, const Ref& ref, int iu, int iv, float fu,
+                                                    float fv, float A0, float A1, float B0, float B1, float c0,
+                                                    float c1, float rmean, float sc, float* acc, float* cnt) {
+  constexpr float kM = 12582912.0f;
+  // validity bounds of the index coordinate relative to texel (iu, iv)
+  const float lu = (float)(-iu), hu = (float)(S.w - 1 - iu), lv = (float)(-iv), hv = (float)(S.h - 1 - iv);
+  const float gxo = ((float)iu + 1.0f) - kM, gyo = ((float)iv + 1.0f) - kM;
+  const float cuo = ((float)iu + 0.5f), cvo = ((float)iv + 0.5f);
+  float ss = 0.f, sss = 0.f, srs = 0.f, sr = 0.f, srr = 0.f, n = 0.f;
+  float cs = 0.f, css = 0.f, crs = 0.f, cr = 0.f, crr = 0.f;
+#pragma unroll 1
+  for (int dy = -H; dy <= H; ++dy) {
+    const auto row = ref.template row<H>(dy);
+    const float fdy = (float)dy;
+    float den = fmaf(fdy, c1, fmaf(-(float)H, c0, 1.0f));
+    float nu = fmaf(fdy, A1, -(float)H * A0);
+    float nv = fmaf(fdy, B1, -(float)H * B0);
+    float r_s = 0.f, r_ss = 0.f, r_rs = 0.f, r_r = 0.f, r_rr = 0.f, r_n = 0.f;
+#pragma unroll 1
+    for (int k = 0; k <= 2 * H; ++k) {
+      const float rinv = rcp_approx(den);
+      const float tu = fmaf(nu, rinv, fu), tv = fmaf(nv, rinv, fv);  // relative index coordinates
+      den += c0;
+      nu += A0;
+      nv += B0;
+      if (!(tu >= lu && tu <= hu && tv >= lv && tv <= hv)) continue;
+      float sv;
+      if constexpr (kMode == kSrcTex) {
+        sv = tex2D<float>(S.tex_lin, tu + cuo, tv + cvo) - sc;
+      } else {
+        const float mu = __fadd_rn(tu - 0.5f, kM), mv = __fadd_rn(tv - 0.5f, kM);
+        const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
+        sv = bilinear<kMode>(S.tex, __fadd_rn(mu, gxo) - 1.0f, __fadd_rn(mv, gyo) - 1.0f, tu - flu, tv - flv) - sc;
+      }
+      const float rv = ((k & 1) ? row.odd(k >> 1) : row.even(k >> 1)) - rmean;
+      r_s += sv;
+      r_ss = fmaf(sv, sv, r_ss);
+      r_rs = fmaf(rv, sv, r_rs);
+      r_r += rv;
+      r_rr = fmaf(rv, rv, r_rr);
+      r_n += 1.0f;
+    }
+    kahan_add(ss, cs, r_s);
+    kahan_add(sss, css, r_ss);
+    kahan_add(srs, crs, r_rs);
+    kahan_add(sr, cr, r_r);
+    kahan_add(srr, crr, r_rr);
+    n += r_n;
+  }
+  acc[0] = sr;
+  acc[1] = srr;
+  acc[2] = ss;
+  acc[3] = sss;
+  acc[4] = srs;
+  *cnt = n;
+}
+
 // The moments of a full window: each row's partial sums in plain FP32 (11
 // terms), the rows combined with Kahan-compensated sums.
 template <int H, int kMode, class Ref>
@@ -459,14 +523,21 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   float acc[5], n;
   const int K = 2 * h + 1;
   const int min_valid = J.min_valid;
-  if (full) {
-    if constexpr (H > 0)
+  if (outside) return bad;
+  if constexpr (H > 0) {
+    if (full) {
       plane_window_fast<H, kMode>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
-    else
-      plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+      return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
+    }
+    if (rw.full && front) {
+      // straddles a source border: masked samples, reference from the tile
+      plane_window_masked<H, kMode>(S, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc, &n);
+      return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
+    }
+  } else if (full) {
+    plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
-  if (outside) return bad;
   plane_window<false, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
 }
