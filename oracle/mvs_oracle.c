@@ -1526,7 +1526,8 @@ static void pm_pixel(const pm_task* T, int x, int y) {
       const double kp = hn[1] * rx + hn[2] * ry + hn[3];
       const double rho = (kn < 0.0 && kp < 0.0) ? hn[0] * kp / kn : -1.0;
       if (!(rho > 0.0)) continue;
-      if (rho == cur[0] && hn[1] == cur[1] && hn[2] == cur[2] && hn[3] == cur[3]) continue;
+      /* the current plane again: same normal, inverse depth within 4e-6 relative */
+      if (hn[1] == cur[1] && hn[2] == cur[2] && hn[3] == cur[3] && fabs(rho - cur[0]) <= 4e-6 * cur[0]) continue;
       const double n[3] = {hn[1], hn[2], hn[3]};
       int32_t sup;
       const double c = pm_eval(T, x, y, rx, ry, rho, n, &sup);

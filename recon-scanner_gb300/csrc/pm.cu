@@ -307,6 +307,11 @@ __global__ void __launch_bounds__(128, 4) k_plane_init(const __grid_constant__ P
   J.support[idx] = (uint8_t)min(c.support, 255);
 }
 
+// Propagation skips a candidate that is the pixel's current plane: same
+// normal bits and an inverse depth within this relative distance (the FP32
+// plane transfer through a chain of neighbours rounds at ~1e-7 per step).
+constexpr float kSamePlaneRel = 4e-6f;
+
 // Adaptive checkerboard regions (other-colour pixels only: dx + dy odd).
 // 4 near "V" regions of 7 pixels and 4 far strips of 11 pixels.
 __constant__ signed char c_near[4][7][2] = {
@@ -403,7 +408,10 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     float rho;
     plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
     if (!(rho > 0.f)) continue;
-    if (rho == cur.x && hn.y == cur.y && hn.z == cur.z && hn.w == cur.w) continue;
+    // the current plane again (same normal, inverse depth within rounding of
+    // the transfer): nothing to learn -- in a converged region most regions
+    // propose exactly this
+    if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) continue;
     const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
