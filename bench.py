@@ -1,23 +1,31 @@
 """Benchmark: depth maps/s of plane-mode PatchMatch MVS on one GB300.
 
-Workload (the headline configuration): one reference view + 8 sources at
+Workload (the headline configuration): the tabletop capture -- 9 views at
 1920x1440, f = 1450 px with Brown-Conrady distortion (k1 = 0.05,
 k2 = -0.01), the tabletop scene (sphere, box, three cylinders on a tilted
-plane, value-noise albedo with 10 % weak-texture patches), 11x11 windows,
-8 iterations, FP32.  A step = one depth map: initialisation, 8 red-black
-iterations, sub-pixel refinement, output.  Images are undistorted on the
-device when staged.
+plane, value-noise albedo with 10 % weak-texture patches) -- each view the
+reference of one depth map with the other 8 as its sources; 11x11 windows,
+8 iterations.  A step = the 9 maps: initialisation, 8 red-black iterations,
+sub-pixel refinement, output.  Images are undistorted on the device when
+staged; the capture's consistency + fusion stage is reported beside it.
 
-  form   -- the chosen form: source images stored as FP16 textures, window
-            samples interpolated by the texture unit; the plain FP32 path
-            (FP32 textures, exact FP32 interpolation) is timed in the same
-            run and reported under "plain_fp32" with its depth agreement;
+  form   -- the chosen form: all maps of the step in one batch (one
+            persistent launch per half-sweep, replayed from a CUDA graph),
+            source images stored as FP16 textures, window samples
+            interpolated by the texture unit; the plain path (FP32 textures,
+            exact FP32 interpolation, one launch per view) is timed in the
+            same run and reported under "plain" with its depth agreement;
   value  -- depth maps/s with the staged inputs resident in HBM; each step
             is timed with CUDA events on the engine's stream and L2 is
             flushed (a 512 MiB write) between steps, outside the events;
   e2e    -- the same metric through the public C ABI from host buffers:
-            stage (H2D of 9 8-bit images + undistortion + textures),
-            run, download (depth, support, confidence, normal, cost), release.
+            stage the capture (H2D of its 8-bit images once each,
+            undistortion, textures), stage the jobs, run, download (depth,
+            support, confidence, normal, cost), release.
+
+Other workloads: --workload small (C1, one 640x480 map), c3 (48 orbit
+references, batched vs per-view), c4 (the differentiation form), c5 (mixed
+precision).
 
 `--impl reference` times the reference algorithm on the host cores instead
 (the CPU oracle restatement of patchmatch_stereo.cpp, all threads) on a
@@ -276,7 +284,21 @@ def run_reference_arm(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 
-def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, sampler=None):
+def stage_capture(M, eng, scenes, cfgs, undistort):
+    """Stage every distinct view of the step once (a capture's views serve as
+    the reference of one map and sources of the others), then one job per
+    scene from the staged images.  Returns (jobs, image ids)."""
+    ids = {}
+    for sc in scenes:
+        for v in [sc.ref] + list(sc.sources):
+            if id(v) not in ids:
+                ids[id(v)] = eng.stage_image(v.image, v.camera.intrinsics_array(), undistort=undistort)
+    jobs = [eng.stage_images(ids[id(sc.ref)], [ids[id(v)] for v in sc.sources], sc.ref.camera.pose_array(),
+                             [v.camera.pose_array() for v in sc.sources], c) for sc, c in zip(scenes, cfgs)]
+    return jobs, list(ids.values())
+
+
+def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, sampler=None, scenes=None):
     """Stage the step's views once, run `warmup` untimed steps, then `steps`
     timed steps (CUDA events on the engine stream around the whole run; L2
     flushed between steps, outside the events).  A step runs every view:
@@ -285,7 +307,10 @@ def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, samp
     import torch
 
     eng = M.Engine(opts)
-    jobs = [eng.stage(v, c, undistort=undistort) for v, c in zip(views, cfgs)]
+    if scenes is not None:
+        jobs, _ = stage_capture(M, eng, scenes, cfgs, undistort)
+    else:
+        jobs = [eng.stage(v, c, undistort=undistort) for v, c in zip(views, cfgs)]
     for _ in range(warmup):
         eng.run_many(jobs)
         eng.synchronize()
@@ -424,7 +449,7 @@ def run_gpu(args):
 
     clk = ClockSampler(local)
     step_ms, sweep_ms, hyps, launches_per_step, maps, st = time_form(M, views, cfgs, opts, args.steps, args.warmup,
-                                                                     flush, world, undistort, clk)
+                                                                     flush, world, undistort, clk, scenes=scenes)
     total_ms = barrier_max(world, float(sum(step_ms)))
     value = world * n_maps * args.steps / (total_ms / 1000.0)
     acc = accuracy(maps, truths)
@@ -434,7 +459,7 @@ def run_gpu(args):
         p_fp16 = False if WORKLOAD != "c3" else args.fp16
         p_interp = 0 if WORKLOAD != "c3" else args.interp
         p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True), args.steps,
-                                                      args.warmup, flush, world, undistort)
+                                                      args.warmup, flush, world, undistort, scenes=scenes)
         p_total = barrier_max(world, float(sum(p_ms)))
         med, p95 = agreement(maps, p_maps)
         plain = {"value": world * n_maps * args.steps / (p_total / 1000.0), "unit": "depth maps/s",
@@ -445,25 +470,36 @@ def run_gpu(args):
 
     # ---- end to end through the C ABI from host buffers ----
     e2e_times = []
+    phases = {"stage": [], "run": [], "download": [], "release": []}
     if args.e2e_steps > 0:
         eng = M.Engine(opts)
         dmh = [M.DepthMap.allocate(sc.ref.camera.width, sc.ref.camera.height) for sc in scenes]
-        for i in range(args.e2e_steps + 1):
+        for it in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            jobs = [eng.stage(v, c, undistort=undistort) for v, c in zip(views, cfgs)]
+            jobs, imgs = stage_capture(M, eng, scenes, cfgs, undistort)
+            eng.synchronize()
+            t1 = time.perf_counter()
             eng.run_many(jobs)
+            eng.synchronize()
+            t2 = time.perf_counter()
             for j, d in zip(jobs, dmh):
                 eng.download(j, d)
+            t3 = time.perf_counter()
             for j in jobs:
                 eng.release(j)
-            t1 = time.perf_counter()
-            if i > 0:
-                e2e_times.append(t1 - t0)
+            for i in imgs:
+                eng.release_image(i)
+            t4 = time.perf_counter()
+            if it > 0:
+                e2e_times.append(t4 - t0)
+                for k, v in zip(phases, (t1 - t0, t2 - t1, t3 - t2, t4 - t3)):
+                    phases[k].append(v * 1e3)
         eng.close()
     e2e_s = barrier_max(world, statistics.mean(e2e_times)) if e2e_times else float("nan")
     e2e_value = world * n_maps / e2e_s
-    h2d = int(sum(sc.ref.image.size + sum(s.image.size for s in sc.sources) for sc in scenes))
+    distinct = {id(v): v for sc in scenes for v in [sc.ref] + list(sc.sources)}
+    h2d = int(sum(v.image.size for v in distinct.values()))
     d2h = int(sum(p * (4 + 1 + 4 + 12 + 4) + 4 for p in pixels))
 
     # ---- roofline of the dominant kernel (the red-black sweep) ----
@@ -503,7 +539,8 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": launches_per_step * args.steps,
             "e2e": {"value": e2e_value, "unit": "depth maps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "ms_by_phase": {k: statistics.mean(v) for k, v in phases.items() if v}},
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved_tflops / peak_tflops, "traffic": traffic,
                          "kernel": "k_plane_sweep",

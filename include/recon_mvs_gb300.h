@@ -316,6 +316,23 @@ RECON_API void recon_mvs_context_destroy(void* ctx);
  * (recon_mvs_undistort) on the device. */
 RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* views, const recon_mvs_config* cfg,
                                            int32_t undistort, int32_t* out_job);
+/* Shared staging for a capture: an image is uploaded once (optionally
+ * undistorted on the device; its intrinsics then become pinhole) and any
+ * number of jobs use it -- as the reference of one map and a source of
+ * others -- through recon_mvs_job_stage_images.  Jobs keep the images they
+ * use alive; recon_mvs_image_release only drops the context's handle.  No
+ * counterpart in the reference (its StageMvs passes the same keyframe
+ * buffers to every PatchMatchStereo call). */
+RECON_API recon_status recon_mvs_image_stage(void* ctx, const uint8_t* gray, int32_t w, int32_t h,
+                                             const recon_camera_intrinsics* intr, int32_t undistort,
+                                             int32_t* out_image);
+RECON_API recon_status recon_mvs_image_release(void* ctx, int32_t image);
+/* A job from staged images: the reference image, num_src source images and
+ * their world -> camera poses (src_poses[k] belongs to src_images[k]). */
+RECON_API recon_status recon_mvs_job_stage_images(void* ctx, int32_t ref_image, int32_t num_src,
+                                                  const int32_t* src_images, const recon_pose* ref_pose,
+                                                  const recon_pose* src_poses, const recon_mvs_config* cfg,
+                                                  int32_t* out_job);
 /* Run PatchMatch (+ refinement per options) on staged jobs, asynchronously
  * on the context's stream.  Plane-mode jobs of one call run as one batch
  * (options.per_view); running the same job list again replays the batch's

@@ -182,15 +182,32 @@ static int hardware_threads() {
 // ---------------------------------------------------------------------------
 // jobs
 // ---------------------------------------------------------------------------
+// One staged image: its device copy (8-bit, or FP32 after on-device
+// undistortion / pre-filtering) and, built on first use, its source form
+// (a texture in the context's storage format) and its reference form
+// ((I - 128) rows, the 2x2-box copy where needed, even / odd column planes).
+// Jobs share images: a capture's view is staged once and serves as the
+// reference of its own map and a source of the others.
+struct StagedImage {
+  int w = 0, h = 0;
+  recon_camera_intrinsics intr{};  // as matched: distortion zeroed when undistorted on the device
+  DevArray<uint8_t> u8;
+  DevArray<float> f32;
+  bool is_f32 = false;
+  std::unique_ptr<Texture> tex;
+  DevArray<float> ref, box, de;
+  bool has_ref = false;
+  const void* dev() const { return is_f32 ? (const void*)f32.p : (const void*)u8.p; }
+};
+
 struct JobData {
   int w = 0, h = 0, num_src = 0;
   recon_mvs_config cfg{};
   recon_mvs_options opts{};
   bool degenerate = false;  // zero baseline or empty depth range: output all-invalid
   double inv_per_px = 0.0;
-  DevArray<uint8_t> ref_u8;
-  DevArray<float> ref, ref_box, ref_de;
-  std::vector<std::unique_ptr<Texture>> tex;
+  std::shared_ptr<StagedImage> ref_img;
+  std::vector<std::shared_ptr<StagedImage>> src_img;
   std::vector<SrcView> host_src;
   DevArray<SrcView> src_table;
   DevArray<float4> hyp;
@@ -278,6 +295,8 @@ struct Context {
   std::map<int, std::unique_ptr<JobData>> jobs;
   int next_id = 1;
   std::unique_ptr<PlanePlan> plan;  // the last batch run, with its captured graph
+  std::map<int, std::shared_ptr<StagedImage>> images;
+  int next_image = 1;
   DevArray<unsigned long long> counter;
   DevArray<uint8_t> stage_u8;
   DevArray<float> stage_f32;
@@ -288,6 +307,9 @@ struct Context {
   DevArray<uint32_t> draws_dev[2];
   DevArray<uint8_t> fire_dev[2];
   cudaEvent_t copy_done[2] = {nullptr, nullptr};
+  // device -> host downloads through two pinned chunks
+  PinnedBuf d2h_buf[2];
+  cudaEvent_t d2h_done[2] = {nullptr, nullptr};
   cudaEvent_t ev_start = nullptr, ev_sweep0 = nullptr, ev_sweep1 = nullptr, ev_end = nullptr;
   recon_mvs_stats stats{};
 
@@ -303,6 +325,7 @@ struct Context {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& e : copy_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : d2h_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CK(cudaEventCreate(&ev_start));
     CK(cudaEventCreate(&ev_sweep0));
     CK(cudaEventCreate(&ev_sweep1));
@@ -315,7 +338,10 @@ struct Context {
     if (stream) cudaStreamSynchronize(stream);
     plan.reset();
     jobs.clear();
+    images.clear();
     for (auto& e : copy_done)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : d2h_done)
       if (e) cudaEventDestroy(e);
     for (auto e : {ev_start, ev_sweep0, ev_sweep1, ev_end})
       if (e) cudaEventDestroy(e);
@@ -459,66 +485,87 @@ static void set_src_transform(SrcView& S, const recon_pose& ref, const recon_pos
   }
 }
 
-static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,
-                     const double* seeds, int num_seeds) {
-  validate_views(v);
+static void zero_distortion(recon_camera_intrinsics* k) { k->k1 = k->k2 = k->k3 = k->p1 = k->p2 = 0.0; }
+
+static std::shared_ptr<StagedImage> stage_image(Context& C, const uint8_t* host, int w, int h,
+                                                const recon_camera_intrinsics& k, bool undistort) {
+  if (!host || w <= 0 || h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "image NULL or empty");
+  auto I = std::make_shared<StagedImage>();
+  I->w = w;
+  I->h = h;
+  I->intr = k;
+  upload_image(C, host, w, h, undistort ? &k : nullptr, I->u8, I->f32, &I->is_f32);
+  if (undistort) zero_distortion(&I->intr);
+  return I;
+}
+
+static void ensure_texture(Context& C, StagedImage& I) {
+  if (I.tex) return;
+  I.tex = std::make_unique<Texture>();
+  make_texture(C, I.dev(), I.is_f32, I.w, I.h, C.opts.storage, *I.tex);
+  CK(cudaStreamSynchronize(C.stream));  // the context's staging buffer is reused
+}
+
+static void ensure_reference(Context& C, StagedImage& I) {
+  if (I.has_ref) return;
+  const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
+  const bool want_box = !plane || C.opts.sampling == 1;
+  const size_t n = (size_t)I.w * I.h;
+  I.ref.alloc(n);
+  if (want_box) I.box.alloc(n);
+  if (I.is_f32)
+    CK(launch_prep_ref_f32(I.f32.p, I.w, I.h, I.ref.p, want_box ? I.box.p : nullptr, C.stream));
+  else
+    CK(launch_prep_ref(I.u8.p, I.w, I.h, I.ref.p, want_box ? I.box.p : nullptr, C.stream));
+  if (plane) {
+    const int half_w = (I.w + 1) / 2;
+    I.de.alloc((size_t)2 * half_w * I.h);
+    CK(launch_deinterleave(C.opts.sampling == 1 ? I.box.p : I.ref.p, I.w, I.h, half_w, I.de.p, C.stream));
+  }
+  I.has_ref = true;
+}
+
+// A job from staged images: the reference, its sources and their poses.
+static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
+                     const std::vector<std::shared_ptr<StagedImage>>& srcs, const recon_pose& ref_pose,
+                     const std::vector<recon_pose>& src_poses, const recon_mvs_config* cfg, const double* seeds,
+                     int num_seeds) {
   if (!cfg) fail(RECON_ERR_INVALID_ARGUMENT, "config is NULL");
   if (cfg->patch_size < 1) fail(RECON_ERR_INVALID_ARGUMENT, "patch_size < 1");
+  if (srcs.empty()) fail(RECON_ERR_INVALID_ARGUMENT, "no source views");
+  if ((int)srcs.size() > kMaxSources) fail(RECON_ERR_INVALID_ARGUMENT, "more than 32 sources");
   C.use();
   auto jd = std::make_unique<JobData>();
   JobData& D = *jd;
-  D.w = v->ref_w;
-  D.h = v->ref_h;
-  D.num_src = v->num_src;
+  D.w = ref->w;
+  D.h = ref->h;
+  D.num_src = (int)srcs.size();
   D.cfg = *cfg;
   D.opts = C.opts;
   const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
   const bool bf16 = C.opts.storage == RECON_MVS_STORAGE_BF16;
-  recon_camera_intrinsics rk = *v->ref_intr;
-  if (plane && !undistort) {
+  const recon_camera_intrinsics rk = ref->intr;
+  if (plane) {
     bool any = distorted(rk);
-    for (int k = 0; k < v->num_src; ++k) any = any || distorted(src_intr(*v, k));
+    for (const auto& I : srcs) any = any || distorted(I->intr);
     if (any) fail(RECON_ERR_INVALID_ARGUMENT, "plane mode needs pinhole images: stage with undistort = 1");
   }
-
-  // ---- reference image ----
-  bool ref_f32 = false;
-  DevArray<float> ref_und;
-  const void* ref_dev = upload_image(C, v->ref_gray, D.w, D.h, undistort ? &rk : nullptr, D.ref_u8, ref_und, &ref_f32);
-  D.ref.alloc((size_t)D.w * D.h);
-  const bool compat = !plane;
-  const bool want_box = compat || C.opts.sampling == 1;
-  if (want_box) D.ref_box.alloc((size_t)D.w * D.h);
-  if (ref_f32)
-    CK(launch_prep_ref_f32((const float*)ref_dev, D.w, D.h, D.ref.p, want_box ? D.ref_box.p : nullptr, C.stream));
-  else
-    CK(launch_prep_ref((const uint8_t*)ref_dev, D.w, D.h, D.ref.p, want_box ? D.ref_box.p : nullptr, C.stream));
-  if (undistort) rk.k1 = rk.k2 = rk.k3 = rk.p1 = rk.p2 = 0.0;
+  ensure_reference(C, *ref);
+  D.ref_img = ref;
   const int half_w = (D.w + 1) / 2;
-  if (plane) {
-    D.ref_de.alloc((size_t)2 * half_w * D.h);
-    CK(launch_deinterleave(C.opts.sampling == 1 ? D.ref_box.p : D.ref.p, D.w, D.h, half_w, D.ref_de.p, C.stream));
-  }
 
   // ---- sources ----
-  D.host_src.resize(v->num_src);
-  for (int k = 0; k < v->num_src; ++k) {
-    recon_camera_intrinsics sk = src_intr(*v, k);
-    const recon_pose& sp = v->src_poses[v->source_indices[k]];
-    bool f32 = false;
-    DevArray<uint8_t> u8;
-    DevArray<float> fl;
-    const void* dev = upload_image(C, v->src_gray[k], v->src_w[k], v->src_h[k], undistort ? &sk : nullptr, u8, fl, &f32);
-    auto T = std::make_unique<Texture>();
-    make_texture(C, dev, f32, v->src_w[k], v->src_h[k], C.opts.storage, *T);
-    CK(cudaStreamSynchronize(C.stream));  // staging buffers are reused
-    if (undistort) sk.k1 = sk.k2 = sk.k3 = sk.p1 = sk.p2 = 0.0;
+  D.host_src.resize(srcs.size());
+  for (size_t k = 0; k < srcs.size(); ++k) {
+    StagedImage& I = *srcs[k];
+    ensure_texture(C, I);
+    const recon_camera_intrinsics& sk = I.intr;
     SrcView& S = D.host_src[k];
     std::memset(&S, 0, sizeof(S));
-    S.tex = T->tex;
-    S.tex_lin = T->tex_lin;
-    S.w = v->src_w[k];
-    S.h = v->src_h[k];
+    S.tex = I.tex->tex;
+    S.tex_lin = I.tex->tex_lin;
+    S.w = I.w;
+    S.h = I.h;
     S.fx = (float)sk.fx;
     S.fy = (float)sk.fy;
     S.cx = (float)sk.cx;
@@ -533,17 +580,20 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
     S.p1 = (float)sk.p1;
     S.p2 = (float)sk.p2;
     S.distorted = distorted(sk) ? 1 : 0;
-    set_src_transform(S, *v->ref_pose, sp, rk);
-    D.src_pose.push_back(sp);
-    D.tex.push_back(std::move(T));
+    set_src_transform(S, ref_pose, src_poses[k], rk);
+    D.src_pose.push_back(src_poses[k]);
   }
-  D.ref_pose = *v->ref_pose;
+  D.src_img = srcs;
+  D.ref_pose = ref_pose;
   D.ref_intr = rk;
-  D.src_table.alloc(v->num_src);
-  CK(cudaMemcpyAsync(D.src_table.p, D.host_src.data(), sizeof(SrcView) * v->num_src, cudaMemcpyHostToDevice, C.stream));
+  D.src_table.alloc(D.num_src);
+  CK(cudaMemcpyAsync(D.src_table.p, D.host_src.data(), sizeof(SrcView) * D.num_src, cudaMemcpyHostToDevice,
+                     C.stream));
 
   // ---- search range and baseline (patchmatch_stereo.cpp:473-485) ----
-  const double baseline = mean_baseline(*v->ref_pose, v->src_poses, v->source_indices, v->num_src);
+  std::vector<int32_t> ident(D.num_src);
+  for (int k = 0; k < D.num_src; ++k) ident[k] = k;
+  const double baseline = mean_baseline(ref_pose, src_poses.data(), ident.data(), D.num_src);
   const double inv_min = depth_to_inverse_depth(cfg->max_depth_m);
   const double inv_max = depth_to_inverse_depth(cfg->min_depth_m);
   D.degenerate = baseline < 1e-9 || !(inv_max > inv_min) || inv_min <= 0.0;
@@ -554,7 +604,7 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   std::memset(&J, 0, sizeof(J));
   J.w = D.w;
   J.h = D.h;
-  J.num_src = v->num_src;
+  J.num_src = D.num_src;
   J.patch_half = cfg->patch_size / 2;
   J.min_valid = cfg->patch_size * cfg->patch_size / 2;
   J.rfx = (float)rk.fx;
@@ -571,13 +621,13 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   J.rk3 = rk.k3;
   J.rp1 = rk.p1;
   J.rp2 = rk.p2;
-  J.ref = D.ref.p;
-  J.ref_box = D.ref_box.p;
-  J.ref_de = D.ref_de.p;
+  J.ref = ref->ref.p;
+  J.ref_box = ref->box.p;
+  J.ref_de = ref->de.p;
   J.ref_half_w = half_w;
   J.half_pixel = (plane && C.opts.sampling == 1) ? 1 : 0;
   J.src_mode = !plane ? kSrcExact : (bf16 ? kSrcBf16 : (C.opts.interp == 1 ? kSrcTex : kSrcExact));
-  J.pref = J.half_pixel ? D.ref_box.p : D.ref.p;
+  J.pref = J.half_pixel ? ref->box.p : ref->ref.p;
   J.src = D.src_table.p;
   J.dinv_min = inv_min;
   J.dinv_max = inv_max;
@@ -647,6 +697,29 @@ static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_confi
   const int id = C.next_id++;
   C.jobs[id] = std::move(jd);
   return id;
+}
+
+// The PatchMatchStereo argument list (reference index contract): every image
+// staged for this job alone.
+static int stage_job(Context& C, const recon_mvs_views* v, const recon_mvs_config* cfg, bool undistort,
+                     const double* seeds, int num_seeds) {
+  validate_views(v);
+  if (!cfg) fail(RECON_ERR_INVALID_ARGUMENT, "config is NULL");
+  C.use();
+  const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
+  if (plane && !undistort) {
+    bool any = distorted(*v->ref_intr);
+    for (int k = 0; k < v->num_src; ++k) any = any || distorted(src_intr(*v, k));
+    if (any) fail(RECON_ERR_INVALID_ARGUMENT, "plane mode needs pinhole images: stage with undistort = 1");
+  }
+  auto ref = stage_image(C, v->ref_gray, v->ref_w, v->ref_h, *v->ref_intr, undistort);
+  std::vector<std::shared_ptr<StagedImage>> srcs;
+  std::vector<recon_pose> poses;
+  for (int k = 0; k < v->num_src; ++k) {
+    srcs.push_back(stage_image(C, v->src_gray[k], v->src_w[k], v->src_h[k], src_intr(*v, k), undistort));
+    poses.push_back(v->src_poses[v->source_indices[k]]);
+  }
+  return build_job(C, ref, srcs, *v->ref_pose, poses, cfg, seeds, num_seeds);
 }
 
 static JobData& get_job(Context& C, int id) {
@@ -1047,6 +1120,36 @@ static void finish_stats(Context& C) {
   cudaGetLastError();
 }
 
+// Device -> pageable host copy through two pinned chunks: the DMA of one
+// chunk overlaps the host copy of the previous one (a direct copy into
+// pageable memory runs at a fraction of the link's rate).  Synchronous.
+static void copy_to_host(Context& C, void* dst, const void* src, size_t bytes) {
+  constexpr size_t kChunk = (size_t)8 << 20;
+  if (bytes <= ((size_t)1 << 16)) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+    return;
+  }
+  for (auto& b : C.d2h_buf) b.alloc(kChunk);
+  const char* s = static_cast<const char*>(src);
+  char* d = static_cast<char*>(dst);
+  auto issue = [&](int k, size_t off) {
+    const size_t n = std::min(kChunk, bytes - off);
+    CK(cudaMemcpyAsync(C.d2h_buf[k].p, s + off, n, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaEventRecord(C.d2h_done[k], C.stream));
+  };
+  issue(0, 0);
+  int k = 0;
+  for (size_t off = 0; off < bytes;) {
+    const size_t n = std::min(kChunk, bytes - off);
+    if (off + n < bytes) issue(k ^ 1, off + n);  // chunk k ^ 1 was copied out last round
+    CK(cudaEventSynchronize(C.d2h_done[k]));
+    std::memcpy(d + off, C.d2h_buf[k].p, n);
+    off += n;
+    k ^= 1;
+  }
+}
+
 static void download_job(Context& C, JobData& D, recon_mvs_depth_map* out, uint32_t* filled) {
   if (!out || !out->depth || !out->support_count || !out->confidence)
     fail(RECON_ERR_INVALID_ARGUMENT, "output depth map arrays NULL");
@@ -1064,16 +1167,16 @@ static void download_job(Context& C, JobData& D, recon_mvs_depth_map* out, uint3
     if (filled) *filled = 0;
     return;
   }
-  CK(cudaMemcpyAsync(out->depth, D.out_depth.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->support_count, D.out_support.p, npx, cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->confidence, D.out_conf.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  copy_to_host(C, out->depth, D.out_depth.p, npx * sizeof(float));
+  copy_to_host(C, out->support_count, D.out_support.p, npx);
+  copy_to_host(C, out->confidence, D.out_conf.p, npx * sizeof(float));
   if (out->normal) {
     if (D.out_normal.p)
-      CK(cudaMemcpyAsync(out->normal, D.out_normal.p, 3 * npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+      copy_to_host(C, out->normal, D.out_normal.p, 3 * npx * sizeof(float));
     else
       std::fill(out->normal, out->normal + 3 * npx, 0.0f);
   }
-  if (out->cost) CK(cudaMemcpyAsync(out->cost, D.out_cost.p, npx * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  if (out->cost) copy_to_host(C, out->cost, D.out_cost.p, npx * sizeof(float));
   unsigned int f = 0;
   CK(cudaMemcpyAsync(&f, D.filled.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
   CK(cudaStreamSynchronize(C.stream));
@@ -1911,6 +2014,53 @@ RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* vie
   return guard([&] {
     if (!ctx || !out_job) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
     *out_job = stage_job(*static_cast<Context*>(ctx), views, cfg, undistort != 0, nullptr, 0);
+  });
+}
+
+RECON_API recon_status recon_mvs_image_stage(void* ctx, const uint8_t* gray, int32_t w, int32_t h,
+                                             const recon_camera_intrinsics* intr, int32_t undistort,
+                                             int32_t* out_image) {
+  return guard([&] {
+    if (!ctx || !intr || !out_image) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    auto I = stage_image(C, gray, w, h, *intr, undistort != 0);
+    CK(cudaStreamSynchronize(C.stream));  // the host image may go away after the call
+    const int id = C.next_image++;
+    C.images[id] = std::move(I);
+    *out_image = id;
+  });
+}
+
+RECON_API recon_status recon_mvs_image_release(void* ctx, int32_t image) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    if (!C.images.erase(image)) fail(RECON_ERR_INVALID_ARGUMENT, "unknown image id");
+  });
+}
+
+RECON_API recon_status recon_mvs_job_stage_images(void* ctx, int32_t ref_image, int32_t num_src,
+                                                  const int32_t* src_images, const recon_pose* ref_pose,
+                                                  const recon_pose* src_poses, const recon_mvs_config* cfg,
+                                                  int32_t* out_job) {
+  return guard([&] {
+    if (!ctx || !src_images || !ref_pose || !src_poses || !out_job) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (num_src < 1) fail(RECON_ERR_INVALID_ARGUMENT, "no source views");
+    Context& C = *static_cast<Context*>(ctx);
+    auto find = [&](int id) {
+      auto it = C.images.find(id);
+      if (it == C.images.end()) fail(RECON_ERR_INVALID_ARGUMENT, "unknown image id");
+      return it->second;
+    };
+    std::vector<std::shared_ptr<StagedImage>> srcs;
+    std::vector<recon_pose> poses(src_poses, src_poses + num_src);
+    for (int k = 0; k < num_src; ++k) {
+      if (src_images[k] == ref_image) fail(RECON_ERR_INVALID_ARGUMENT, "the reference is listed as a source");
+      srcs.push_back(find(src_images[k]));
+    }
+    *out_job = build_job(C, find(ref_image), srcs, *ref_pose, poses, cfg, nullptr, 0);
   });
 }
 

@@ -174,6 +174,12 @@ _SIGS = {
     "recon_mvs_job_run": (C.c_int, [C.c_void_p, C.c_int32]),
     "recon_mvs_jobs_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
     "recon_mvs_job_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(DepthMapC), C.POINTER(C.c_uint32)]),
+    "recon_mvs_image_stage": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32,
+                                        C.POINTER(Intrinsics), C.c_int32, C.POINTER(C.c_int32)]),
+    "recon_mvs_image_release": (C.c_int, [C.c_void_p, C.c_int32]),
+    "recon_mvs_job_stage_images": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                             C.POINTER(Pose), C.POINTER(Pose), C.POINTER(MvsConfig),
+                                             C.POINTER(C.c_int32)]),
     "recon_mvs_job_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -460,6 +466,7 @@ class Engine:
         _check(_lib().recon_mvs_context_create(C.byref(self.options), C.byref(self.ctx)))
         self._keep = {}
         self._nsrc = {}
+        self._img_shape = {}
 
     def stage(self, views: ViewArgs, config: MvsConfig, undistort=False) -> int:
         job = C.c_int32()
@@ -484,6 +491,32 @@ class Engine:
         _check(_lib().recon_mvs_job_download(self.ctx, job, C.byref(st), C.byref(f)))
         dm.filled = int(f.value)
         return dm
+
+    def stage_image(self, gray, intr, undistort=False) -> int:
+        """Upload one image once for any number of jobs (intr: 11 values or
+        Intrinsics)."""
+        g = np.ascontiguousarray(gray, np.uint8)
+        k = intrinsics(intr)
+        out = C.c_int32()
+        _check(_lib().recon_mvs_image_stage(self.ctx, _ptr(g, C.c_uint8), g.shape[1], g.shape[0], C.byref(k),
+                                            int(undistort), C.byref(out)))
+        self._img_shape[out.value] = g.shape
+        return out.value
+
+    def release_image(self, image: int):
+        _check(_lib().recon_mvs_image_release(self.ctx, image))
+
+    def stage_images(self, ref_image: int, src_images, ref_pose, src_poses, config: MvsConfig) -> int:
+        """A job from staged images (poses: 13 values or Pose each)."""
+        ids = np.ascontiguousarray(src_images, np.int32)
+        ps = (Pose * len(ids))(*[pose(p) for p in src_poses])
+        rp = pose(ref_pose)
+        job = C.c_int32()
+        _check(_lib().recon_mvs_job_stage_images(self.ctx, ref_image, len(ids), _ptr(ids, C.c_int32), C.byref(rp),
+                                                 C.cast(ps, C.POINTER(Pose)), C.byref(config), C.byref(job)))
+        self._keep[job.value] = self._img_shape[ref_image]
+        self._nsrc[job.value] = len(ids)
+        return job.value
 
     def adjoint(self, job: int, px, py, depth, angles, gn=False, pose=False):
         """The adjoint at hypotheses (pixel, depth, theta/phi).  Returns

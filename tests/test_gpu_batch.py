@@ -115,3 +115,35 @@ def test_batch_larger_than_one_table(mvs):
     assert st.last_sweep_launches == 4  # two groups x one iteration x two colours
     for m in batch:
         np.testing.assert_array_equal(m.depth, single[0].depth)
+
+
+def test_shared_image_staging_matches_per_job_staging(mvs):
+    """A capture staged once (each view the reference of one job and a source
+    of the others) gives the same maps as staging every job's images."""
+    import synthetic as S
+
+    cap = S.tabletop(width=200, height=150, f=1450.0 * 200 / 1920, num_sources=3, seed=6)
+    scenes = [S.as_reference(cap, k) for k in range(len(cap.views))]
+    opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0)
+
+    def cfg(sc):
+        return mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=3, patch_size=11)
+
+    eng = mvs.Engine(opts)
+    own = [eng.stage(views_of(mvs, sc), cfg(sc), undistort=True) for sc in scenes]
+    eng.run_many(own)
+    a = [eng.download(j) for j in own]
+    eng.close()
+    eng = mvs.Engine(opts)
+    ids = [eng.stage_image(v.image, v.camera.intrinsics_array(), undistort=True) for v in cap.views]
+    jobs = []
+    for k, sc in enumerate(scenes):
+        others = [i for i in range(len(cap.views)) if i != k]
+        jobs.append(eng.stage_images(ids[k], [ids[i] for i in others], cap.views[k].camera.pose_array(),
+                                     [cap.views[i].camera.pose_array() for i in others], cfg(sc)))
+    for i in ids:
+        eng.release_image(i)  # the jobs keep their images
+    eng.run_many(jobs)
+    b = [eng.download(j) for j in jobs]
+    eng.close()
+    assert_same(b, a, "shared staging")
