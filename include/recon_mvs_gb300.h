@@ -367,6 +367,36 @@ RECON_API recon_status recon_mvs_job_recover_poses(void* ctx, int32_t job, int32
                                                    const int32_t* py, const double* depth, const double* angles,
                                                    int32_t iterations, recon_pose* out_src_poses,
                                                    double* out_cost);
+/* ---- the MVS stage over a capture (Orchestrator::StageMvs) ---- */
+
+typedef int32_t (*recon_mvs_cancel_fn)(void* user);              /* nonzero: cancel */
+typedef void (*recon_mvs_progress_fn)(void* user, double fraction); /* maps done / maps */
+typedef struct recon_mvs_stage_params {
+  int32_t undistort;              /* stage images with on-device undistortion (plane mode needs it
+                                     for distorted cameras) */
+  int32_t batch_size;             /* maps per batched run; 0 = every map in one batch */
+  int32_t consistency_views;      /* 0 = fuse every map as StageMvs does; n > 0 = fuse only pixels
+                                     consistent with >= n other maps */
+  float consistency_rel_depth;    /* |z_back - z| / z bound of the consistency test */
+  float consistency_reproj_px;    /* reprojection bound of the consistency test, pixels */
+  recon_mvs_cancel_fn cancel;     /* optional, checked before every batch */
+  recon_mvs_progress_fn progress; /* optional, called after every batch */
+  void* user;
+} recon_mvs_stage_params;
+
+/* Orchestrator::StageMvs (orchestrator.cpp:942-1071) on the batched engine:
+ * keyframes with their gray images (NULL = none), world -> camera poses and
+ * intrinsics; per keyframe the sources of SelectSourceViews (without itself
+ * and image-less frames, at most num_views); PatchMatch (+ the context's
+ * refinement; RefineSubpixel in COMPAT mode) in batches; maps with nothing
+ * filled dropped; fusion of the rest on the device into out_cloud (freed
+ * with recon_mvs_point_cloud_free).  RECON_ERR_MVS_NO_DEPTH: fewer than two
+ * keyframes or no map; RECON_ERR_CANCELLED: the cancel callback said so. */
+RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray, const int32_t* width,
+                                           const int32_t* height, const recon_pose* poses,
+                                           const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                                           const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
+                                           recon_mvs_point_cloud* out_cloud, int32_t* out_maps);
 /* Copy a finished job's map to the host (synchronises). */
 RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out,
                                               uint32_t* out_filled);

@@ -1751,6 +1751,53 @@ RECON_API recon_status recon_mvs_refine_subpixel(const recon_mvs_views* views, c
   });
 }
 
+// One device-resident depth map with its camera (consistency, fusion).
+struct DevMap {
+  int w, h;
+  const float* depth;
+  recon_camera_intrinsics intr;
+  recon_pose pose;
+};
+
+// Geometric consistency of `ref` against `others` on the device: per pixel
+// the number of consistent maps (out_count) and count >= min_views (out_keep).
+static void consistency_device(Context& C, const DevMap& ref, const std::vector<DevMap>& others, float rel_depth_max,
+                               float reproj_px_max, int min_views, uint8_t* out_count, uint8_t* out_keep) {
+  ConsistencyRef cr{ref.w, ref.h, ref.depth, (float)ref.intr.fx, (float)ref.intr.fy, (float)ref.intr.cx,
+                    (float)ref.intr.cy};
+  std::vector<ConsistencySrc> srcs;
+  for (const DevMap& o : others) {
+    ConsistencySrc cs;
+    std::memset(&cs, 0, sizeof(cs));
+    cs.w = o.w;
+    cs.h = o.h;
+    cs.depth = o.depth;
+    cs.fx = (float)o.intr.fx;
+    cs.fy = (float)o.intr.fy;
+    cs.cx = (float)o.intr.cx;
+    cs.cy = (float)o.intr.cy;
+    double A[9], b[3], Ai[9], bi[3];
+    relative_transform(ref.pose, o.pose, A, b);
+    relative_transform(o.pose, ref.pose, Ai, bi);
+    for (int i = 0; i < 9; ++i) {
+      cs.A[i] = (float)A[i];
+      cs.Ai[i] = (float)Ai[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+      cs.b[i] = (float)b[i];
+      cs.bi[i] = (float)bi[i];
+    }
+    srcs.push_back(cs);
+  }
+  DevArray<ConsistencySrc> ds;
+  ds.alloc(std::max<size_t>(1, srcs.size()));
+  if (!srcs.empty())
+    CK(cudaMemcpyAsync(ds.p, srcs.data(), srcs.size() * sizeof(ConsistencySrc), cudaMemcpyHostToDevice, C.stream));
+  CK(launch_consistency(cr, ds.p, (int)srcs.size(), rel_depth_max, reproj_px_max, min_views, out_count, out_keep,
+                        C.stream));
+  CK(cudaStreamSynchronize(C.stream));  // the descriptor table is freed on return
+}
+
 RECON_API recon_status recon_mvs_geometric_consistency(const recon_mvs_depth_map* maps, const recon_pose* poses,
                                                        const recon_camera_intrinsics* intr, int32_t num_maps,
                                                        int32_t ref_index, float rel_depth_max, float reproj_px_max,
@@ -1770,42 +1817,16 @@ RECON_API recon_status recon_mvs_geometric_consistency(const recon_mvs_depth_map
     }
     const recon_mvs_depth_map& R = maps[ref_index];
     if (!R.depth) fail(RECON_ERR_INVALID_ARGUMENT, "reference map NULL");
-    ConsistencyRef cr{R.width, R.height, dev[ref_index]->p, (float)intr[ref_index].fx, (float)intr[ref_index].fy,
-                      (float)intr[ref_index].cx, (float)intr[ref_index].cy};
-    std::vector<ConsistencySrc> srcs;
-    for (int s = 0; s < num_maps; ++s) {
-      if (s == ref_index || !maps[s].depth) continue;
-      ConsistencySrc cs;
-      std::memset(&cs, 0, sizeof(cs));
-      cs.w = maps[s].width;
-      cs.h = maps[s].height;
-      cs.depth = dev[s]->p;
-      cs.fx = (float)intr[s].fx;
-      cs.fy = (float)intr[s].fy;
-      cs.cx = (float)intr[s].cx;
-      cs.cy = (float)intr[s].cy;
-      double A[9], b[3], Ai[9], bi[3];
-      relative_transform(poses[ref_index], poses[s], A, b);
-      relative_transform(poses[s], poses[ref_index], Ai, bi);
-      for (int i = 0; i < 9; ++i) {
-        cs.A[i] = (float)A[i];
-        cs.Ai[i] = (float)Ai[i];
-      }
-      for (int i = 0; i < 3; ++i) {
-        cs.b[i] = (float)b[i];
-        cs.bi[i] = (float)bi[i];
-      }
-      srcs.push_back(cs);
-    }
-    DevArray<ConsistencySrc> ds;
-    ds.alloc(std::max<size_t>(1, srcs.size()));
-    if (!srcs.empty())
-      CK(cudaMemcpyAsync(ds.p, srcs.data(), srcs.size() * sizeof(ConsistencySrc), cudaMemcpyHostToDevice, C.stream));
+    std::vector<DevMap> others;
+    for (int s = 0; s < num_maps; ++s)
+      if (s != ref_index && maps[s].depth)
+        others.push_back(DevMap{maps[s].width, maps[s].height, dev[s]->p, intr[s], poses[s]});
     const size_t n = (size_t)R.width * R.height;
     DevArray<uint8_t> dc, dk;
     dc.alloc(n);
     dk.alloc(n);
-    CK(launch_consistency(cr, ds.p, (int)srcs.size(), rel_depth_max, reproj_px_max, min_views, dc.p, dk.p, C.stream));
+    consistency_device(C, DevMap{R.width, R.height, dev[ref_index]->p, intr[ref_index], poses[ref_index]}, others,
+                       rel_depth_max, reproj_px_max, min_views, dc.p, dk.p);
     CK(cudaMemcpyAsync(out_count, dc.p, n, cudaMemcpyDeviceToHost, C.stream));
     CK(cudaMemcpyAsync(out_keep, dk.p, n, cudaMemcpyDeviceToHost, C.stream));
     CK(cudaStreamSynchronize(C.stream));
@@ -1823,6 +1844,135 @@ RECON_API void recon_mvs_point_cloud_free(recon_mvs_point_cloud* c) {
   std::memset(c, 0, sizeof(*c));
 }
 
+static FuseMap fuse_map(int w, int h, const float* depth, const uint8_t* support, const float* conf,
+                        const uint8_t* keep, const recon_camera_intrinsics& k, const recon_pose& pose) {
+  FuseMap M;
+  std::memset(&M, 0, sizeof(M));
+  M.w = w;
+  M.h = h;
+  M.depth = depth;
+  M.support = support;
+  M.conf = conf;
+  M.keep = keep;
+  M.fx = k.fx;
+  M.fy = k.fy;
+  M.cx = k.cx;
+  M.cy = k.cy;
+  M.k1 = k.k1;
+  M.k2 = k.k2;
+  M.k3 = k.k3;
+  M.p1 = k.p1;
+  M.p2 = k.p2;
+  for (int i = 0; i < 9; ++i) M.R[i] = pose.r[i];
+  for (int i = 0; i < 3; ++i) M.t[i] = pose.t[i];
+  return M;
+}
+
+// FuseDepthMaps on device-resident maps (FuseMap: device pointers, camera):
+// the reference's voxel keys in FP64, a hash table of first occurrences,
+// buckets of points per voxel in the reference's insertion order, sequential
+// FP64 sums.  The cloud is malloc-allocated (recon_mvs_point_cloud_free).
+static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_mvs_config& cfg,
+                      recon_mvs_point_cloud* out) {
+  std::memset(out, 0, sizeof(*out));
+  if (maps.empty() || cfg.fusion_voxel_size_m <= 0.0) return;
+  int64_t total = 0;
+  std::vector<int64_t> base(maps.size());
+  for (size_t m = 0; m < maps.size(); ++m) {
+    base[m] = total;
+    total += (int64_t)maps[m].w * maps[m].h;
+  }
+  if (total == 0) return;
+  DevArray<unsigned long long> key, tkey, tfirst;
+  DevArray<double> pos, nrm;
+  DevArray<float> conf;
+  DevArray<uint8_t> valid;
+  DevArray<int> slot_of, err;
+  DevArray<unsigned int> tcount, flag, vid_of, slot_vid, scratch;
+  key.alloc(total);
+  pos.alloc(3 * total);
+  nrm.alloc(3 * total);
+  conf.alloc(total);
+  valid.alloc(total);
+  slot_of.alloc(total);
+  flag.alloc(total);
+  vid_of.alloc(total);
+  err.alloc(1);
+  uint64_t cap = 1024;
+  while (cap < 2 * (uint64_t)total) cap <<= 1;
+  tkey.alloc(cap);
+  tfirst.alloc(cap);
+  tcount.alloc(cap);
+  slot_vid.alloc(cap);
+  CK(cudaMemsetAsync(tkey.p, 0x7F, cap * sizeof(unsigned long long), C.stream));
+  CK(cudaMemsetAsync(tfirst.p, 0xFF, cap * sizeof(unsigned long long), C.stream));
+  CK(cudaMemsetAsync(tcount.p, 0, cap * sizeof(unsigned int), C.stream));
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), C.stream));
+  const FuseParams P{cfg.fusion_voxel_size_m, cfg.photo_threshold, cfg.min_view_consistency};
+  for (size_t m = 0; m < maps.size(); ++m)
+    CK(launch_fuse_points(maps[m], base[m], P, key.p, pos.p, nrm.p, conf.p, valid.p, C.stream));
+  CK(cudaMemsetAsync(slot_of.p, 0xFF, total * sizeof(int), C.stream));  // -1: no slot
+  CK(launch_fuse_insert(total, key.p, valid.p, tkey.p, tcount.p, tfirst.p, cap - 1, slot_of.p, err.p, C.stream));
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  if (herr) fail(RECON_ERR_INTERNAL, "voxel hash table overflow");
+  CK(launch_fuse_flags(total, valid.p, slot_of.p, tfirst.p, flag.p, C.stream));
+  scratch.alloc(scan_scratch_elems(total));
+  CK(exclusive_scan_u32(flag.p, vid_of.p, total, scratch.p, C.stream));
+  unsigned int last_vid = 0, last_flag = 0;
+  CK(cudaMemcpyAsync(&last_vid, vid_of.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(&last_flag, flag.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  const unsigned int nvox = last_vid + last_flag;
+  if (nvox == 0) return;
+  DevArray<unsigned int> vcount, voffset, cursor;
+  vcount.alloc(nvox);
+  voffset.alloc(nvox);
+  cursor.alloc(nvox);
+  CK(launch_fuse_voxels(total, flag.p, vid_of.p, slot_of.p, tcount.p, slot_vid.p, vcount.p, C.stream));
+  scratch.alloc(std::max<int64_t>(scan_scratch_elems(nvox), (int64_t)scratch.n));
+  CK(exclusive_scan_u32(vcount.p, voffset.p, nvox, scratch.p, C.stream));
+  unsigned int last_off = 0, last_cnt = 0;
+  CK(cudaMemcpyAsync(&last_off, voffset.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(&last_cnt, vcount.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemsetAsync(cursor.p, 0, nvox * sizeof(unsigned int), C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+  const int64_t npts = (int64_t)last_off + last_cnt;
+  DevArray<int64_t> bucket;
+  bucket.alloc(npts);
+  CK(launch_fuse_scatter(total, valid.p, slot_of.p, slot_vid.p, voffset.p, cursor.p, bucket.p, C.stream));
+  DevArray<unsigned long long> okey;
+  DevArray<double> opos, onrm;
+  DevArray<float> oconf;
+  DevArray<unsigned int> ocount;
+  okey.alloc(nvox);
+  opos.alloc(3 * (size_t)nvox);
+  onrm.alloc(3 * (size_t)nvox);
+  oconf.alloc(nvox);
+  ocount.alloc(nvox);
+  CK(launch_fuse_reduce(nvox, voffset.p, vcount.p, bucket.p, key.p, pos.p, nrm.p, conf.p, okey.p, opos.p, onrm.p,
+                        oconf.p, ocount.p, C.stream));
+  out->count = nvox;
+  out->positions = (double*)std::malloc(3 * sizeof(double) * nvox);
+  out->normals = (double*)std::malloc(3 * sizeof(double) * nvox);
+  out->colors = (float*)std::calloc(3 * (size_t)nvox, sizeof(float));
+  out->confidences = (float*)std::malloc(sizeof(float) * nvox);
+  out->keys = (int64_t*)std::malloc(sizeof(int64_t) * nvox);
+  out->counts = (uint32_t*)std::malloc(sizeof(uint32_t) * nvox);
+  if (!out->positions || !out->normals || !out->colors || !out->confidences || !out->keys || !out->counts) {
+    recon_mvs_point_cloud_free(out);
+    fail(RECON_ERR_OUT_OF_MEMORY, "point cloud allocation failed");
+  }
+  CK(cudaMemcpyAsync(out->positions, opos.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->normals, onrm.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->confidences, oconf.p, sizeof(float) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->keys, okey.p, sizeof(int64_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->counts, ocount.p, sizeof(uint32_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaStreamSynchronize(C.stream));
+
+}
+
 RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const recon_pose* poses,
                                       const recon_camera_intrinsics* intr, int32_t num_maps,
                                       const recon_mvs_config* cfg, const uint8_t* const* keep_masks,
@@ -1835,41 +1985,9 @@ RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const rec
     if (cfg->fusion_voxel_size_m <= 0.0) return;
     Context& C = default_context(nullptr);
     C.use();
-    int64_t total = 0;
-    std::vector<int64_t> base(num_maps);
-    for (int m = 0; m < num_maps; ++m) {
-      base[m] = total;
-      if (maps[m].depth) total += (int64_t)maps[m].width * maps[m].height;
-    }
-    if (total == 0) return;
-    DevArray<unsigned long long> key, tkey, tfirst;
-    DevArray<double> pos, nrm;
-    DevArray<float> conf;
-    DevArray<uint8_t> valid;
-    DevArray<int> slot_of, err;
-    DevArray<unsigned int> tcount, flag, vid_of, slot_vid, scratch;
-    key.alloc(total);
-    pos.alloc(3 * total);
-    nrm.alloc(3 * total);
-    conf.alloc(total);
-    valid.alloc(total);
-    slot_of.alloc(total);
-    flag.alloc(total);
-    vid_of.alloc(total);
-    err.alloc(1);
-    uint64_t cap = 1024;
-    while (cap < 2 * (uint64_t)total) cap <<= 1;
-    tkey.alloc(cap);
-    tfirst.alloc(cap);
-    tcount.alloc(cap);
-    slot_vid.alloc(cap);
-    CK(cudaMemsetAsync(tkey.p, 0x7F, cap * sizeof(unsigned long long), C.stream));
-    CK(cudaMemsetAsync(tfirst.p, 0xFF, cap * sizeof(unsigned long long), C.stream));
-    CK(cudaMemsetAsync(tcount.p, 0, cap * sizeof(unsigned int), C.stream));
-    CK(cudaMemsetAsync(err.p, 0, sizeof(int), C.stream));
-    FuseParams P{cfg->fusion_voxel_size_m, cfg->photo_threshold, cfg->min_view_consistency};
     std::vector<std::unique_ptr<DevArray<float>>> dd, dc;
     std::vector<std::unique_ptr<DevArray<uint8_t>>> dsup, dkeep;
+    std::vector<FuseMap> fm;
     for (int m = 0; m < num_maps; ++m) {
       if (!maps[m].depth) continue;
       if (!maps[m].support_count || !maps[m].confidence) fail(RECON_ERR_INVALID_ARGUMENT, "map arrays NULL");
@@ -1890,87 +2008,10 @@ RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const rec
         CK(cudaMemcpyAsync(dkeep.back()->p, keep_masks[m], n, cudaMemcpyHostToDevice, C.stream));
         keep = dkeep.back()->p;
       }
-      const recon_camera_intrinsics& k = intr[m];
-      FuseMap M;
-      std::memset(&M, 0, sizeof(M));
-      M.w = maps[m].width;
-      M.h = maps[m].height;
-      M.depth = dd.back()->p;
-      M.support = dsup.back()->p;
-      M.conf = dc.back()->p;
-      M.keep = keep;
-      M.fx = k.fx;
-      M.fy = k.fy;
-      M.cx = k.cx;
-      M.cy = k.cy;
-      M.k1 = k.k1;
-      M.k2 = k.k2;
-      M.k3 = k.k3;
-      M.p1 = k.p1;
-      M.p2 = k.p2;
-      for (int i = 0; i < 9; ++i) M.R[i] = poses[m].r[i];
-      for (int i = 0; i < 3; ++i) M.t[i] = poses[m].t[i];
-      CK(launch_fuse_points(M, base[m], P, key.p, pos.p, nrm.p, conf.p, valid.p, C.stream));
+      fm.push_back(fuse_map(maps[m].width, maps[m].height, dd.back()->p, dsup.back()->p, dc.back()->p, keep,
+                            intr[m], poses[m]));
     }
-    CK(cudaMemsetAsync(slot_of.p, 0xFF, total * sizeof(int), C.stream));  // -1: no slot
-    CK(launch_fuse_insert(total, key.p, valid.p, tkey.p, tcount.p, tfirst.p, cap - 1, slot_of.p, err.p, C.stream));
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaStreamSynchronize(C.stream));
-    if (herr) fail(RECON_ERR_INTERNAL, "voxel hash table overflow");
-    CK(launch_fuse_flags(total, valid.p, slot_of.p, tfirst.p, flag.p, C.stream));
-    scratch.alloc(scan_scratch_elems(total));
-    CK(exclusive_scan_u32(flag.p, vid_of.p, total, scratch.p, C.stream));
-    unsigned int last_vid = 0, last_flag = 0;
-    CK(cudaMemcpyAsync(&last_vid, vid_of.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(&last_flag, flag.p + total - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaStreamSynchronize(C.stream));
-    const unsigned int nvox = last_vid + last_flag;
-    if (nvox == 0) return;
-    DevArray<unsigned int> vcount, voffset, cursor;
-    vcount.alloc(nvox);
-    voffset.alloc(nvox);
-    cursor.alloc(nvox);
-    CK(launch_fuse_voxels(total, flag.p, vid_of.p, slot_of.p, tcount.p, slot_vid.p, vcount.p, C.stream));
-    scratch.alloc(std::max<int64_t>(scan_scratch_elems(nvox), (int64_t)scratch.n));
-    CK(exclusive_scan_u32(vcount.p, voffset.p, nvox, scratch.p, C.stream));
-    unsigned int last_off = 0, last_cnt = 0;
-    CK(cudaMemcpyAsync(&last_off, voffset.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(&last_cnt, vcount.p + nvox - 1, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemsetAsync(cursor.p, 0, nvox * sizeof(unsigned int), C.stream));
-    CK(cudaStreamSynchronize(C.stream));
-    const int64_t npts = (int64_t)last_off + last_cnt;
-    DevArray<int64_t> bucket;
-    bucket.alloc(npts);
-    CK(launch_fuse_scatter(total, valid.p, slot_of.p, slot_vid.p, voffset.p, cursor.p, bucket.p, C.stream));
-    DevArray<unsigned long long> okey;
-    DevArray<double> opos, onrm;
-    DevArray<float> oconf;
-    DevArray<unsigned int> ocount;
-    okey.alloc(nvox);
-    opos.alloc(3 * (size_t)nvox);
-    onrm.alloc(3 * (size_t)nvox);
-    oconf.alloc(nvox);
-    ocount.alloc(nvox);
-    CK(launch_fuse_reduce(nvox, voffset.p, vcount.p, bucket.p, key.p, pos.p, nrm.p, conf.p, okey.p, opos.p, onrm.p,
-                          oconf.p, ocount.p, C.stream));
-    out->count = nvox;
-    out->positions = (double*)std::malloc(3 * sizeof(double) * nvox);
-    out->normals = (double*)std::malloc(3 * sizeof(double) * nvox);
-    out->colors = (float*)std::calloc(3 * (size_t)nvox, sizeof(float));
-    out->confidences = (float*)std::malloc(sizeof(float) * nvox);
-    out->keys = (int64_t*)std::malloc(sizeof(int64_t) * nvox);
-    out->counts = (uint32_t*)std::malloc(sizeof(uint32_t) * nvox);
-    if (!out->positions || !out->normals || !out->colors || !out->confidences || !out->keys || !out->counts) {
-      recon_mvs_point_cloud_free(out);
-      fail(RECON_ERR_OUT_OF_MEMORY, "point cloud allocation failed");
-    }
-    CK(cudaMemcpyAsync(out->positions, opos.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(out->normals, onrm.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(out->confidences, oconf.p, sizeof(float) * nvox, cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(out->keys, okey.p, sizeof(int64_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaMemcpyAsync(out->counts, ocount.p, sizeof(uint32_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
-    CK(cudaStreamSynchronize(C.stream));
+    fuse_maps(C, fm, *cfg, out);
   });
 }
 
@@ -2077,6 +2118,124 @@ RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_
     if (!ctx || (!jobs && n > 0)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
     Context& C = *static_cast<Context*>(ctx);
     run_jobs(C, std::vector<int>(jobs, jobs + n));
+  });
+}
+
+// ---- the MVS stage over a whole capture ------------------------------------
+// Orchestrator::StageMvs (orchestrator.cpp:942-1071) restated for the batched
+// engine: every keyframe image staged once; per keyframe the sources of
+// SelectSourceViews without itself and without image-less frames, at most
+// num_views; the maps run in batches with the cancel check before each batch
+// and a progress report after it; maps with nothing filled are dropped; the
+// rest are fused (optionally behind the geometric-consistency filter) on the
+// device.
+RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray, const int32_t* width,
+                                           const int32_t* height, const recon_pose* poses,
+                                           const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                                           const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
+                                           recon_mvs_point_cloud* out_cloud, int32_t* out_maps) {
+  return guard([&] {
+    if (!ctx || !gray || !width || !height || !poses || !intr || !cfg || !out_cloud)
+      fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out_cloud, 0, sizeof(*out_cloud));
+    if (out_maps) *out_maps = 0;
+    recon_mvs_stage_params P;
+    std::memset(&P, 0, sizeof(P));
+    if (params) P = *params;
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    if (num_keyframes < 2) fail(RECON_ERR_MVS_NO_DEPTH, "fewer than two keyframes");
+    const int N = num_keyframes;
+    std::vector<std::shared_ptr<StagedImage>> img(N);
+    for (int r = 0; r < N; ++r)
+      if (gray[r]) img[r] = stage_image(C, gray[r], width[r], height[r], intr[r], P.undistort != 0);
+
+    struct Jobs {  // every job of the stage is released on the way out
+      Context& C;
+      std::vector<int> ids;
+      ~Jobs() {
+        for (int id : ids) erase_job(C, id);
+      }
+    } jobs{C, {}};
+    std::vector<int> ref_of;  // keyframe of each job
+    std::vector<int32_t> sel(N);
+    for (int r = 0; r < N; ++r) {
+      if (!img[r]) continue;
+      int32_t cnt = 0;
+      const recon_status st = recon_mvs_select_source_views(&poses[r], poses, N, &intr[r], cfg, sel.data(), N, &cnt);
+      if (st != RECON_OK) fail(st, "source view selection failed");
+      std::vector<int> kept;
+      for (int k = 0; k < cnt; ++k) {
+        const int si = sel[k];
+        if (si == r || si < 0 || si >= N || !img[si]) continue;
+        kept.push_back(si);
+      }
+      if ((int)kept.size() > cfg->num_views) kept.resize(std::max(0, cfg->num_views));
+      if (kept.empty()) continue;
+      std::vector<std::shared_ptr<StagedImage>> srcs;
+      std::vector<recon_pose> sp;
+      for (int si : kept) {
+        srcs.push_back(img[si]);
+        sp.push_back(poses[si]);
+      }
+      jobs.ids.push_back(build_job(C, img[r], srcs, poses[r], sp, cfg, nullptr, 0));
+      ref_of.push_back(r);
+    }
+    const int nj = (int)jobs.ids.size();
+    const int batch = P.batch_size > 0 ? P.batch_size : std::max(1, nj);
+    const bool compat = C.opts.mode != RECON_MVS_MODE_PLANE;
+    DevArray<unsigned int> refined;
+    refined.alloc(1);
+    std::vector<unsigned int> filled(nj, 0);
+    for (int start = 0; start < nj; start += batch) {
+      if (P.cancel && P.cancel(P.user)) fail(RECON_ERR_CANCELLED, "cancelled");
+      const int end = std::min(nj, start + batch);
+      run_jobs(C, std::vector<int>(jobs.ids.begin() + start, jobs.ids.begin() + end));
+      for (int j = start; j < end; ++j) {
+        JobData& D = get_job(C, jobs.ids[j]);
+        if (D.degenerate) continue;
+        if (compat)  // PatchMatchStereo is followed by RefineSubpixel (orchestrator.cpp:1041-1044)
+          CK(launch_compat_refine(D.J, D.out_depth.p, D.out_conf.p, D.inv_per_px, cfg->subpixel_fit_points,
+                                  cfg->subpixel_iterations, refined.p, nullptr, nullptr, C.stream));
+        CK(cudaMemcpyAsync(&filled[j], D.filled.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
+      }
+      CK(cudaStreamSynchronize(C.stream));
+      if (P.progress) P.progress(P.user, (double)end / (double)nj);
+    }
+    std::vector<int> produced;
+    for (int j = 0; j < nj; ++j)
+      if (filled[j] > 0 && !get_job(C, jobs.ids[j]).degenerate) produced.push_back(j);
+    if (produced.empty()) fail(RECON_ERR_MVS_NO_DEPTH, "no depth map produced");
+
+    std::vector<std::unique_ptr<DevArray<uint8_t>>> keep(produced.size());
+    if (P.consistency_views > 0) {
+      std::vector<DevMap> dm;
+      for (int j : produced) {
+        const JobData& D = get_job(C, jobs.ids[j]);
+        dm.push_back(DevMap{D.w, D.h, D.out_depth.p, img[ref_of[j]]->intr, poses[ref_of[j]]});
+      }
+      DevArray<uint8_t> count;
+      for (size_t i = 0; i < produced.size(); ++i) {
+        std::vector<DevMap> others;
+        for (size_t q = 0; q < produced.size(); ++q)
+          if (q != i) others.push_back(dm[q]);
+        const size_t n = (size_t)dm[i].w * dm[i].h;
+        count.alloc(n);
+        keep[i] = std::make_unique<DevArray<uint8_t>>();
+        keep[i]->alloc(n);
+        consistency_device(C, dm[i], others, P.consistency_rel_depth, P.consistency_reproj_px, P.consistency_views,
+                           count.p, keep[i]->p);
+      }
+    }
+    std::vector<FuseMap> fm;
+    for (size_t i = 0; i < produced.size(); ++i) {
+      const JobData& D = get_job(C, jobs.ids[produced[i]]);
+      const int r = ref_of[produced[i]];
+      fm.push_back(fuse_map(D.w, D.h, D.out_depth.p, D.out_support.p, D.out_conf.p, keep[i] ? keep[i]->p : nullptr,
+                            img[r]->intr, poses[r]));
+    }
+    fuse_maps(C, fm, *cfg, out_cloud);
+    if (out_maps) *out_maps = (int32_t)produced.size();
   });
 }
 

@@ -124,6 +124,16 @@ class Stats(C.Structure):
                 ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
+CANCEL_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p)
+PROGRESS_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double)
+
+
+class StageParams(C.Structure):
+    _fields_ = [("undistort", C.c_int32), ("batch_size", C.c_int32), ("consistency_views", C.c_int32),
+                ("consistency_rel_depth", C.c_float), ("consistency_reproj_px", C.c_float),
+                ("cancel", CANCEL_FN), ("progress", PROGRESS_FN), ("user", C.c_void_p)]
+
+
 class MvsError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"recon_status {status}: {msg}")
@@ -180,6 +190,10 @@ _SIGS = {
     "recon_mvs_job_stage_images": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                              C.POINTER(Pose), C.POINTER(Pose), C.POINTER(MvsConfig),
                                              C.POINTER(C.c_int32)]),
+    "recon_mvs_stage_run": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32), C.POINTER(Pose), C.POINTER(Intrinsics), C.c_int32,
+                                      C.POINTER(MvsConfig), C.POINTER(StageParams), C.POINTER(PointCloudC),
+                                      C.POINTER(C.c_int32)]),
     "recon_mvs_job_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -399,6 +413,12 @@ def FuseDepthMaps(depth_maps, poses, intrinsics_list, config: MvsConfig, keep_ma
     pc = PointCloudC()
     _check(_lib().recon_mvs_fuse(arr, C.cast(ps, C.POINTER(Pose)), C.cast(ks, C.POINTER(Intrinsics)), n,
                                  C.byref(config), keep_ptrs, C.byref(pc)))
+    del keeps  # the masks had to outlive the call
+    return _take_cloud(pc)
+
+
+def _take_cloud(pc: PointCloudC) -> PointCloud:
+    """Copy a library-allocated cloud into numpy arrays and free it."""
     try:
         m = int(pc.count)
         if m == 0:
@@ -411,7 +431,6 @@ def FuseDepthMaps(depth_maps, poses, intrinsics_list, config: MvsConfig, keep_ma
                           cp(pc.keys, 1, np.int64), cp(pc.counts, 1, np.uint32))
     finally:
         _lib().recon_mvs_point_cloud_free(C.byref(pc))
-        del keeps
 
 
 # ----------------------------------------------------------------------------
@@ -553,6 +572,30 @@ class Engine:
                                                   poses, _ptr(hist, C.c_double)))
         out = np.array([[*p.r, *p.t] for p in poses], np.float64)
         return out, hist
+
+    def stage_run(self, images, poses, intrinsics_list, config: MvsConfig, undistort=False, batch_size=0,
+                  consistency_views=0, rel_depth=0.01, reproj_px=1.0, cancel=None, progress=None):
+        """Orchestrator::StageMvs on the batched engine: keyframe images (None
+        = no image), poses and intrinsics -> (PointCloud, maps fused).
+        cancel() -> bool and progress(fraction) are optional callables."""
+        n = len(images)
+        imgs = [None if im is None else np.ascontiguousarray(im, np.uint8) for im in images]
+        ptrs = (C.POINTER(C.c_uint8) * max(1, n))(*[None if im is None else _ptr(im, C.c_uint8) for im in imgs])
+        w = np.asarray([0 if im is None else im.shape[1] for im in imgs] or [0], np.int32)
+        h = np.asarray([0 if im is None else im.shape[0] for im in imgs] or [0], np.int32)
+        ps = (Pose * max(1, n))(*[pose(p) for p in poses])
+        ks = (Intrinsics * max(1, n))(*[intrinsics(k) for k in intrinsics_list])
+        cb_cancel = CANCEL_FN((lambda _u: 1 if cancel() else 0) if cancel else 0)
+        cb_progress = PROGRESS_FN((lambda _u, f: progress(f)) if progress else 0)
+        prm = StageParams(int(undistort), int(batch_size), int(consistency_views), rel_depth, reproj_px,
+                          cb_cancel, cb_progress, None)
+        pc = PointCloudC()
+        maps = C.c_int32()
+        _check(_lib().recon_mvs_stage_run(self.ctx, C.cast(ptrs, C.POINTER(C.POINTER(C.c_uint8))),
+                                          _ptr(w, C.c_int32), _ptr(h, C.c_int32), C.cast(ps, C.POINTER(Pose)),
+                                          C.cast(ks, C.POINTER(Intrinsics)), n, C.byref(config), C.byref(prm),
+                                          C.byref(pc), C.byref(maps)))
+        return _take_cloud(pc), maps.value
 
     def release(self, job: int):
         _check(_lib().recon_mvs_job_release(self.ctx, job))

@@ -1,0 +1,109 @@
+"""GPU: the MVS stage over a capture (recon_mvs_stage_run), the batched
+restatement of Orchestrator::StageMvs (orchestrator.cpp:942-1071).
+
+Bar: the fused cloud is bit-identical to the same pipeline assembled from
+the per-job entry points (SelectSourceViews without the keyframe itself, at
+most num_views sources, one PatchMatch job per keyframe, FuseDepthMaps);
+cancel and progress callbacks behave as StageMvs's (cancel checked before
+each batch -> RECON_ERR_CANCELLED; progress after each batch); fewer than two
+keyframes -> RECON_ERR_MVS_NO_DEPTH.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RECON_ERR_CANCELLED = 5
+RECON_ERR_MVS_NO_DEPTH = 500
+
+
+@pytest.fixture(scope="module")
+def mvs():
+    import recon_mvs
+
+    recon_mvs.load_library()
+    return recon_mvs
+
+
+@pytest.fixture(scope="module")
+def capture():
+    import synthetic as S
+
+    cap = S.tabletop(width=200, height=150, f=1450.0 * 200 / 1920, num_sources=4, k1=0.0, k2=0.0, seed=8)
+    return cap
+
+
+def cfg_of(mvs, cap):
+    return mvs.MvsConfig(min_depth_m=cap.min_depth, max_depth_m=cap.max_depth, iterations=3, patch_size=11,
+                         num_views=3, fusion_voxel_size_m=0.002)
+
+
+def test_stage_run_matches_assembled_pipeline(mvs, capture):
+    cams = [v.camera for v in capture.views]
+    imgs = [v.image for v in capture.views]
+    poses = [c.pose_array() for c in cams]
+    intr = [c.intrinsics_array() for c in cams]
+    cfg = cfg_of(mvs, capture)
+    opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0)
+
+    eng = mvs.Engine(opts)
+    fractions = []
+    cloud, nmaps = eng.stage_run(imgs, poses, intr, cfg, batch_size=2, progress=fractions.append)
+    eng.close()
+
+    eng = mvs.Engine(opts)
+    maps, mposes, mintr = [], [], []
+    for r in range(len(cams)):
+        sel = [i for i in mvs.SelectSourceViews(poses[r], poses, intr[r], cfg) if i != r][: cfg.num_views]
+        if not sel:
+            continue
+        views = mvs.ViewArgs.from_cameras(imgs[r], [imgs[i] for i in sel], cams[r], [cams[i] for i in sel])
+        j = eng.stage(views, cfg)
+        eng.run(j)
+        dm = eng.download(j)
+        eng.release(j)
+        if dm.filled > 0:
+            maps.append(dm)
+            mposes.append(poses[r])
+            mintr.append(intr[r])
+    eng.close()
+    want = mvs.FuseDepthMaps(maps, mposes, mintr, cfg)
+    print("maps", nmaps, "points", cloud.size(), "progress", fractions)
+    assert nmaps == len(maps)
+    assert cloud.size() == want.size() > 1000
+    np.testing.assert_array_equal(cloud.keys, want.keys)
+    np.testing.assert_array_equal(cloud.counts, want.counts)
+    np.testing.assert_array_equal(cloud.positions, want.positions)
+    np.testing.assert_array_equal(cloud.normals, want.normals)
+    assert fractions == pytest.approx([2 / nmaps, 4 / nmaps, 1.0])
+
+
+def test_stage_run_consistency_filter_drops_points(mvs, capture):
+    cams = [v.camera for v in capture.views]
+    args = ([v.image for v in capture.views], [c.pose_array() for c in cams], [c.intrinsics_array() for c in cams],
+            cfg_of(mvs, capture))
+    eng = mvs.Engine(mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0))
+    all_pts, _ = eng.stage_run(*args)
+    kept, _ = eng.stage_run(*args, consistency_views=2, rel_depth=0.01, reproj_px=1.0)
+    eng.close()
+    print("points", all_pts.size(), "consistent", kept.size())
+    assert 0 < kept.size() < all_pts.size()
+
+
+def test_stage_run_cancel_and_no_depth(mvs, capture):
+    cams = [v.camera for v in capture.views]
+    imgs = [v.image for v in capture.views]
+    poses = [c.pose_array() for c in cams]
+    intr = [c.intrinsics_array() for c in cams]
+    cfg = cfg_of(mvs, capture)
+    eng = mvs.Engine(mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0))
+    with pytest.raises(mvs.MvsError) as e:
+        eng.stage_run(imgs, poses, intr, cfg, cancel=lambda: True)
+    assert e.value.status == RECON_ERR_CANCELLED
+    with pytest.raises(mvs.MvsError) as e:
+        eng.stage_run(imgs[:1], poses[:1], intr[:1], cfg)
+    assert e.value.status == RECON_ERR_MVS_NO_DEPTH
+    # the context stays usable
+    cloud, n = eng.stage_run(imgs, poses, intr, cfg)
+    eng.close()
+    assert n > 0 and cloud.size() > 0
