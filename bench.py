@@ -419,6 +419,28 @@ def fuse_capture(M, scenes, maps, rel=0.01, reproj=1.0, min_views=3):
             "timing": "host wall clock: 9 consistency calls + fusion, host buffers in and out"}
 
 
+def stage_capture_run(M, scenes, opts):
+    """The whole MVS stage of the capture through one public call
+    (recon_mvs_stage_run: host images in, fused cloud out): staging with
+    on-device undistortion, SelectSourceViews (num_views = 8), one batched run,
+    consistency (>= 3 views, 1 px, 1 %) and fusion on the device.  Host wall
+    clock; the first call (autotune, module load) is excluded."""
+    cams = [sc.ref.camera for sc in scenes]
+    imgs = [sc.ref.image for sc in scenes]
+    cfg = M.MvsConfig(min_depth_m=scenes[0].min_depth, max_depth_m=scenes[0].max_depth, iterations=ITERS,
+                      patch_size=K, subpixel_iterations=4, num_views=S_SRC)
+    eng = M.Engine(opts)
+    args = (imgs, [c.pose_array() for c in cams], [c.intrinsics_array() for c in cams], cfg)
+    kw = dict(undistort=True, consistency_views=3, rel_depth=0.01, reproj_px=1.0)
+    eng.stage_run(*args, **kw)
+    t0 = time.perf_counter()
+    cloud, nmaps = eng.stage_run(*args, **kw)
+    secs = time.perf_counter() - t0
+    eng.close()
+    return {"seconds": secs, "maps": nmaps, "points": int(cloud.size()), "maps_per_s": nmaps / secs,
+            "call": "recon_mvs_stage_run, host images in, fused cloud out"}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -552,6 +574,7 @@ def run_gpu(args):
             "accuracy": acc, "plain": plain, "clocks": clk.summary()}
     if WORKLOAD == "c2" and not args.no_fusion:
         line["fusion"] = fuse_capture(M, scenes, maps)
+        line["stage"] = stage_capture_run(M, scenes, opts)
     if rank == 0 and not args.no_cpu_baseline:
         secs, threads, note = cpu_reference_sample(scenes[0])
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
