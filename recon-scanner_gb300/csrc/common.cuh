@@ -152,6 +152,10 @@ struct SrcView {
   double bd[3];
 };
 
+// Columns of one reference-tile plane staged by a sweep block: the warp's 32
+// same-colour pixels + 8 margin each side (a TMA box row of 192 bytes).
+constexpr int kTileCols = 48;
+
 // Source read modes of the plane-mode kernels (Job::src_mode).
 constexpr int kSrcExact = 0, kSrcTex = 1, kSrcBf16 = 2;
 
@@ -166,8 +170,9 @@ struct Job {
   double rk1, rk2, rk3, rp1, rp2;
   const float* ref;      // (I - 128), row-major w x h
   const float* ref_box;  // compat: 2x2 box average of (I - 128), (w-1) x (h-1) used
-  const float* ref_de;   // plane mode: even / odd column planes of pref, [2][h][ref_half_w]
+  const float* ref_de;   // plane mode: even / odd column planes of pref, [2][h][ref_pitch], ref_half_w used
   int ref_half_w;
+  int ref_pitch;         // row pitch of ref_de in floats: ref_half_w rounded up to 4 (16-byte rows for TMA)
   // plane mode sampling convention: 0 = pixel centres (reference window =
   // pixels, source index = coordinate - 0.5); 1 = the reference's own
   // (window at x + 0.5 + dx with index == coordinate, i.e. the 2x2 box image,

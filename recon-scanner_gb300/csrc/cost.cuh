@@ -306,7 +306,7 @@ struct GlobalRef {
 // Shared-memory tile of the reference image stored as even / odd column
 // planes, so that the 32 lanes of a warp (32 same-colour pixels of one row,
 // two columns apart) read consecutive words: conflict-free.
-constexpr int kTileCols = 48;  // plane columns: the warp's 32 + 8 margin each side
+
 struct TileRow {
   const float* a;
   const float* b;

@@ -23,6 +23,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "kernels.h"
 #include "recon_mvs_gb300.h"
 
@@ -196,6 +198,7 @@ struct StagedImage {
   bool is_f32 = false;
   std::unique_ptr<Texture> tex;
   DevArray<float> ref, box, de;
+  int de_pitch = 0;  // floats per row of `de` (a multiple of 4: 16-byte rows for TMA)
   bool has_ref = false;
   const void* dev() const { return is_f32 ? (const void*)f32.p : (const void*)u8.p; }
 };
@@ -269,6 +272,7 @@ struct PlaneGroup {
   std::unique_ptr<PlaneBatch> sweep[kNumRowChoices];  // 64-column x rows sweep tiles
   std::vector<int> active;  // active[it] = jobs with more than `it` iterations
   DevArray<int> queues;     // one work counter per half-sweep
+  DevArray<CUtensorMap> tmaps[kNumRowChoices];  // per row choice, one per job (windows with H > 0)
   int rows = 4, ctas_per_sm = 1, grid = 1;
 
   int nj() const { return (int)jobs.size(); }
@@ -298,6 +302,7 @@ struct Context {
   std::map<int, std::shared_ptr<StagedImage>> images;
   int next_image = 1;
   DevArray<unsigned long long> counter;
+  DevArray<int> err;  // device-side failure flag (a TMA wait that ran out)
   DevArray<uint8_t> stage_u8;
   DevArray<float> stage_f32;
   DevArray<uint8_t> stage_tex;
@@ -332,6 +337,8 @@ struct Context {
     CK(cudaEventCreate(&ev_end));
     counter.alloc(1);
     CK(cudaMemsetAsync(counter.p, 0, sizeof(unsigned long long), stream));
+    err.alloc(1);
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), stream));
   }
   ~Context() {
     cudaSetDevice(device);
@@ -519,8 +526,10 @@ static void ensure_reference(Context& C, StagedImage& I) {
     CK(launch_prep_ref(I.u8.p, I.w, I.h, I.ref.p, want_box ? I.box.p : nullptr, C.stream));
   if (plane) {
     const int half_w = (I.w + 1) / 2;
-    I.de.alloc((size_t)2 * half_w * I.h);
-    CK(launch_deinterleave(C.opts.sampling == 1 ? I.box.p : I.ref.p, I.w, I.h, half_w, I.de.p, C.stream));
+    I.de_pitch = (half_w + 3) & ~3;
+    I.de.alloc((size_t)2 * I.de_pitch * I.h);
+    CK(launch_deinterleave(C.opts.sampling == 1 ? I.box.p : I.ref.p, I.w, I.h, half_w, I.de_pitch, I.de.p,
+                           C.stream));
   }
   I.has_ref = true;
 }
@@ -625,6 +634,7 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
   J.ref_box = ref->box.p;
   J.ref_de = ref->de.p;
   J.ref_half_w = half_w;
+  J.ref_pitch = ref->de_pitch;
   J.half_pixel = (plane && C.opts.sampling == 1) ? 1 : 0;
   J.src_mode = !plane ? kSrcExact : (bf16 ? kSrcBf16 : (C.opts.interp == 1 ? kSrcTex : kSrcExact));
   J.pref = J.half_pixel ? ref->box.p : ref->ref.p;
@@ -738,6 +748,29 @@ static JobData& get_job(Context& C, int id) {
 // (options.per_view = 1) launches the same kernels once per view instead,
 // without a graph: the comparison the batched form is measured against.
 
+// The TMA view of a job's reference planes: a 3-D tensor {half_w, h, 2} of
+// FP32 with 16-byte row pitch, read in boxes of 48 columns x box_rows rows x
+// both planes (what one sweep tile stages), zeros outside.
+static void encode_ref_tile_map(const JobData& D, int box_rows, CUtensorMap* out) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn) fail(RECON_ERR_MVS_GPU_FAILURE, "cuTensorMapEncodeTiled unavailable");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  const Job& J = D.J;
+  const cuuint64_t dims[3] = {(cuuint64_t)J.ref_half_w, (cuuint64_t)J.h, 2};
+  const cuuint64_t strides[2] = {(cuuint64_t)J.ref_pitch * sizeof(float),
+                                 (cuuint64_t)J.ref_pitch * sizeof(float) * (cuuint64_t)J.h};
+  const cuuint32_t box[3] = {(cuuint32_t)kTileCols, (cuuint32_t)box_rows, 2};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(J.ref_de), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(RECON_ERR_MVS_GPU_FAILURE, "cuTensorMapEncodeTiled failed");
+}
+
 static void build_group(Context& C, PlaneGroup& G) {
   std::stable_sort(G.jobs.begin(), G.jobs.end(), [](const JobData* a, const JobData* b) {
     if (a->cfg.iterations != b->cfg.iterations) return a->cfg.iterations > b->cfg.iterations;
@@ -773,6 +806,16 @@ static void build_group(Context& C, PlaneGroup& G) {
     add(*G.pix, (long long)((D.w + 31) / 32) * ((D.h + 3) / 4));
     for (int r = 0; r < kNumRowChoices; ++r)
       add(*G.sweep[r], (long long)((D.w + 63) / 64) * ((D.h + kRowChoices[r] - 1) / kRowChoices[r]));
+  }
+  G.pix->err = C.err.p;
+  for (int r = 0; r < kNumRowChoices; ++r) {
+    G.sweep[r]->err = C.err.p;
+    if (G.patch_half != 5 && G.patch_half != 3) continue;  // the generic window reads global memory
+    std::vector<CUtensorMap> maps(n);
+    for (int j = 0; j < n; ++j) encode_ref_tile_map(*G.jobs[j], kRowChoices[r] + 2 * G.patch_half, &maps[j]);
+    G.tmaps[r].alloc(n);
+    CK(cudaMemcpy(G.tmaps[r].p, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice));
+    G.sweep[r]->tmaps = G.tmaps[r].p;
   }
   G.active.assign(std::max(G.max_iters, 1), 0);
   for (int it = 0; it < G.max_iters; ++it)
@@ -1113,6 +1156,17 @@ static void erase_job(Context& C, int id) {
   C.jobs.erase(id);
 }
 
+// A device-side failure (a TMA wait that ran out) becomes MVS_GPU_FAILURE;
+// the flag is cleared so the context stays usable.
+static void check_device_error(Context& C) {
+  int e = 0;
+  CK(cudaMemcpy(&e, C.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    CK(cudaMemset(C.err.p, 0, sizeof(int)));
+    fail(RECON_ERR_MVS_GPU_FAILURE, "a tile copy did not complete (TMA wait limit reached)");
+  }
+}
+
 static void finish_stats(Context& C) {
   float ms = 0.f, sw = 0.f;
   if (cudaEventElapsedTime(&ms, C.ev_start, C.ev_end) == cudaSuccess) C.stats.last_run_ms = ms;
@@ -1180,6 +1234,7 @@ static void download_job(Context& C, JobData& D, recon_mvs_depth_map* out, uint3
   unsigned int f = 0;
   CK(cudaMemcpyAsync(&f, D.filled.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, C.stream));
   CK(cudaStreamSynchronize(C.stream));
+  check_device_error(C);
   finish_stats(C);
   unsigned long long ev = 0;
   CK(cudaMemcpy(&ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_fp16.h>
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -64,6 +65,10 @@ struct PlaneBatch {
   Job jobs[kBatchJobs];
   int start[kBatchJobs + 1];
   int njobs;
+  // sweeps: one TMA tensor map per job over its ref_de planes (device memory,
+  // 64-byte aligned), box = 48 columns x (rows + 2H) rows x 2 planes
+  const CUtensorMap* tmaps;
+  int* err;  // set when a TMA wait runs out (the launch then stops early)
 };
 static_assert(sizeof(PlaneBatch) + 64 <= 32764, "PlaneBatch exceeds the kernel-parameter limit");
 cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int max_src, int* queues, int num_queues,
@@ -103,7 +108,7 @@ cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t 
                             cudaStream_t st);
 cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                                   cudaStream_t st);
-cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, float* out, cudaStream_t st);
+cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, int pitch, float* out, cudaStream_t st);
 cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);
 cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,
                                int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,

@@ -455,6 +455,45 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
   J.support[idx] = (uint8_t)min(cur_sup, 255);
 }
 
+// ---- TMA staging of the reference tile ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// The 3-D box {x, y, z} of `map` into shared memory, completion signalled
+// on `bar` (expecting `bytes`).  x is a multiple of 8 floats (32 bytes), y
+// may be negative or past the end: TMA fills zeros there.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar,
+                                            uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Waits for phase `parity` of `bar`, giving up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
+  for (int i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+constexpr int kTmaWaitPolls = 1 << 22;
+
 // One red-black half-sweep over a whole batch: a persistent kernel (grid =
 // resident blocks) whose blocks pull work items -- 64-column x R-row tiles,
 // R = blockDim.y -- from an atomic counter until the batch is exhausted.  A
@@ -470,12 +509,19 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
                                               int iter) {
   extern __shared__ float2 smem[];
   constexpr int kHalo = H > 0 ? H : 1;
-  __shared__ float tile[2][kMaxTileRows + 2 * kHalo][kTileCols];
+  __shared__ __align__(128) float tile[2 * (kMaxTileRows + 2 * kHalo) * kTileCols];
+  __shared__ __align__(8) uint64_t bar;
   __shared__ int s_item;
   const int R = (int)blockDim.y;
   const int nthreads = 32 * R;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const PCache pc{smem, nthreads, tid};
+  const int box_rows = R + 2 * H;
+  if constexpr (H > 0) {
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+  }
+  uint32_t phase = 0;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(queue, 1);
     __syncthreads();
@@ -490,23 +536,28 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
     const int parity = (y + color) & 1;
     const int x = bx * 64 + 2 * (int)threadIdx.x + parity;
     if constexpr (H > 0) {
-      const int i0 = bx * 32 - 8, r0 = by * R - H;
-      for (int p = 0; p < 2; ++p)
-        for (int rr = threadIdx.y; rr < R + 2 * H; rr += R) {
-          const int row = r0 + rr;
-          const bool row_ok = row >= 0 && row < J.h;
-          const float* src = J.ref_de + ((size_t)p * J.h + (row_ok ? row : 0)) * J.ref_half_w;
-          for (int c = threadIdx.x; c < kTileCols; c += 32) {
-            const int col = i0 + c;
-            tile[p][rr][c] = (row_ok && col >= 0 && col < J.ref_half_w) ? src[col] : 0.f;
-          }
+      // the tile: planes [2][box_rows][48] of ref_de from column bx*32 - 8 and
+      // row by*R - H, one TMA box (zeros outside the image)
+      if (tid == 0)
+        tma_load_3d(tile, B.tmaps + j, bx * 32 - 8, by * R - H, 0, &bar,
+                    (uint32_t)(2 * box_rows * kTileCols * sizeof(float)));
+      const bool ok = mbar_wait(&bar, phase, kTmaWaitPolls);
+      phase ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        // give the copy one more bounded chance to land before leaving
+        if (tid == 0) {
+          atomicExch(B.err, 1);
+          mbar_wait(&bar, phase ^ 1u, kTmaWaitPolls);
         }
-      __syncthreads();
+        break;
+      }
     }
     if (x < J.w && y < J.h) {
       if constexpr (H > 0) {
-        const TileRef ref{parity ? &tile[1][0][0] : &tile[0][0][0], parity ? &tile[0][0][0] : &tile[1][0][0],
-                          (int)threadIdx.x, parity, (int)threadIdx.y};
+        const float* plane0 = tile;
+        const float* plane1 = tile + box_rows * kTileCols;
+        const TileRef ref{parity ? plane1 : plane0, parity ? plane0 : plane1, (int)threadIdx.x, parity,
+                          (int)threadIdx.y};
         const RefWindow rw = tile_window<H>(J, ref, x, y);
         sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
       } else {
@@ -965,14 +1016,15 @@ __global__ void k_prep_ref(const uint8_t* __restrict__ img, int w, int h, float*
 }
 
 // Even / odd column planes of the (I - 128) reference image:
-// out[p][y][i] = ref[y][2i + p]  (0 past the right edge).
-__global__ void k_deinterleave(const float* __restrict__ ref, int w, int h, int half_w, float* out) {
+// out[p][y][i] = ref[y][2i + p] for i < half_w (0 past the right edge), rows
+// of `pitch` floats (the padding is zero).
+__global__ void k_deinterleave(const float* __restrict__ ref, int w, int h, int half_w, int pitch, float* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= half_w || y >= h) return;
+  if (i >= pitch || y >= h) return;
   for (int p = 0; p < 2; ++p) {
     const int x = 2 * i + p;
-    out[((size_t)p * h + y) * half_w + i] = x < w ? ref[(size_t)y * w + x] : 0.f;
+    out[((size_t)p * h + y) * pitch + i] = (i < half_w && x < w) ? ref[(size_t)y * w + x] : 0.f;
   }
 }
 
@@ -1265,9 +1317,9 @@ cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const u
   return cudaGetLastError();
 }
 
-cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, float* out, cudaStream_t st) {
+cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, int pitch, float* out, cudaStream_t st) {
   const dim3 b(32, 8);
-  k_deinterleave<<<grid2d(half_w, h, b), b, 0, st>>>(ref, w, h, half_w, out);
+  k_deinterleave<<<grid2d(pitch, h, b), b, 0, st>>>(ref, w, h, half_w, pitch, out);
   return cudaGetLastError();
 }
 
