@@ -12,9 +12,11 @@ staged; the capture's consistency + fusion stage is reported beside it.
   form   -- the chosen form: all maps of the step in one batch (one
             persistent launch per half-sweep, replayed from a CUDA graph),
             source images stored as FP16 textures, window samples
-            interpolated by the texture unit; the plain path (FP32 textures,
-            exact FP32 interpolation, one launch per view) is timed in the
-            same run and reported under "plain" with its depth agreement;
+            interpolated by the texture unit, Gauss-Newton refinement from
+            the adjoint; the plain path (FP32 textures, exact FP32
+            interpolation, one launch per view, the reference's
+            golden-section refinement) is timed in the same run and reported
+            under "plain" with its depth agreement;
   value  -- depth maps/s with the staged inputs resident in HBM; each step
             is timed with CUDA events on the engine's stream and L2 is
             flushed (a 512 MiB write) between steps, outside the events;
@@ -462,11 +464,11 @@ def run_gpu(args):
     # pixel-weighted sources per map: the FLOP model's S for mixed batches
     s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
     flop_per_hyp = s_eff * (K * K * 26 + 30) + 40
-    mk = lambda fp16, interp, per_view: M.Options(
+    mk = lambda fp16, interp, per_view, refine: M.Options(
         mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
-        refine=1, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
+        refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
         tile_rows=args.tile_rows)
-    opts = mk(args.fp16, args.interp, args.per_view)
+    opts = mk(args.fp16, args.interp, args.per_view, args.refine)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
     clk = ClockSampler(local)
@@ -480,13 +482,14 @@ def run_gpu(args):
     if not args.plain and not args.chosen_only:
         p_fp16 = False if WORKLOAD != "c3" else args.fp16
         p_interp = 0 if WORKLOAD != "c3" else args.interp
-        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True), args.steps,
+        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True, 1), args.steps,
                                                       args.warmup, flush, world, undistort, scenes=scenes)
         p_total = barrier_max(world, float(sum(p_ms)))
         med, p95 = agreement(maps, p_maps)
         plain = {"value": world * n_maps * args.steps / (p_total / 1000.0), "unit": "depth maps/s",
                  "ms_per_step": p_total / args.steps, "storage": "fp16" if p_fp16 else "fp32",
                  "interp": "texture-unit" if p_interp else "exact fp32", "launch": "one launch per view",
+                 "refine": "golden section on the inverse depth (the reference's schedule)",
                  "gpu_launches_per_step": p_launches, "accuracy": accuracy(p_maps, truths),
                  "chosen_vs_plain_median_rel_depth_diff": med, "chosen_vs_plain_p95_rel_depth_diff": p95}
 
@@ -539,7 +542,8 @@ def run_gpu(args):
                 f"{WORKLOAD}{'_per_view' if args.per_view else ''}")
 
     form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
-            f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}")
+            f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
+            f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}")
     if WORKLOAD == "c2":
         wl = (f"tabletop capture: 9 views {W}x{H} (k1=0.05, k2=-0.01, undistorted on the device), each the "
               f"reference of one map with the other {S_SRC} as sources")
@@ -870,6 +874,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--best-k", type=int, default=4)
+    ap.add_argument("--refine", type=int, default=None,
+                    help="chosen form's refinement: 1 golden section, 2 Gauss-Newton from the adjoint (default)")
     ap.add_argument("--fp16", action="store_true", default=None)
     ap.add_argument("--plain", action="store_true",
                     help="time only the plain path: FP32 storage, exact FP32 interpolation")
@@ -887,6 +893,8 @@ def main():
     set_workload(args.workload)
     # the chosen form (default): FP16 storage + texture-unit interpolation;
     # the plain FP32 path is timed beside it unless --plain asks for it alone
+    if args.refine is None:
+        args.refine = 1 if (args.plain or args.workload == "c3") else 2
     if args.plain:
         args.fp16, args.interp, args.per_view = False, 0, True
     elif args.workload == "c3":

@@ -134,8 +134,9 @@ typedef struct recon_mvs_options {
   int32_t storage;    /* recon_mvs_storage */
   int32_t best_k;     /* plane mode: views averaged per hypothesis, <= 8; 0 = all valid */
   int32_t refine;     /* plane mode refinement after the sweeps: 0 none; 1 golden-section search of
-                         the inverse depth (the reference's schedule); 2 Gauss-Newton on depth and
-                         normal driven by the adjoint (recon_mvs_job_adjoint) */
+                         the inverse depth (the reference's schedule, subpixel_iterations steps);
+                         2 one Gauss-Newton step on depth and normal driven by the adjoint
+                         (recon_mvs_job_adjoint), kept only if the cost falls */
   uint64_t seed;      /* plane mode random stream */
   int32_t device;     /* CUDA device ordinal */
   int32_t sampling;   /* plane mode: 0 = pixel-centre windows; 1 = the reference's convention

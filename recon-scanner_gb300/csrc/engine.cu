@@ -693,7 +693,12 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
       J.seed_gx = gx;
     }
     J.iterations = cfg->iterations;
-    J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0) ? cfg->subpixel_iterations : 0;
+    // golden section: subpixel_iterations steps (the reference's schedule);
+    // Gauss-Newton: one Levenberg-Marquardt step (up to four damping
+    // retries) -- further steps did not lower the error at the measured
+    // image noise, and each costs about one golden-section search
+    J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0) ? (C.opts.refine == 2 ? 1 : cfg->subpixel_iterations)
+                                                                     : 0;
     J.refine_mode = C.opts.refine;
     J.inv_per_px = (float)D.inv_per_px;
     J.out_depth = D.out_depth.p;
