@@ -556,8 +556,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 storage)" if args.fp16 else "f32",
             "data": "synthetic (seeded scenes, analytic truth)",
-            "config": {"workload": f"{wl}; {K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}, "
-                                   f"golden-section refine",
+            "config": {"workload": f"{wl}; {K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}",
                        "maps_per_step": n_maps, "megapixels_per_step": sum(pixels) / 1e6,
                        "form": form, "tile_rows": st.tile_rows, "ctas_per_sm": st.ctas_per_sm,
                        "prefilter": bool(args.prefilter), "sampling": args.sampling,
