@@ -327,6 +327,12 @@ RECON_API recon_status recon_mvs_job_stage(void* ctx, const recon_mvs_views* vie
 RECON_API recon_status recon_mvs_image_stage(void* ctx, const uint8_t* gray, int32_t w, int32_t h,
                                              const recon_camera_intrinsics* intr, int32_t undistort,
                                              int32_t* out_image);
+/* A BGRA8 camera frame (rows `stride` bytes apart) staged as its gray image:
+ * the conversion of BgraToGray (orchestrator.cpp:53-67, (77 R + 150 G + 29 B)
+ * >> 8) runs on the device after the upload, then as recon_mvs_image_stage. */
+RECON_API recon_status recon_mvs_image_stage_bgra(void* ctx, const uint8_t* bgra, int32_t w, int32_t h,
+                                                  int32_t stride, const recon_camera_intrinsics* intr,
+                                                  int32_t undistort, int32_t* out_image);
 RECON_API recon_status recon_mvs_image_release(void* ctx, int32_t image);
 /* A job from staged images: the reference image, num_src source images and
  * their world -> camera poses (src_poses[k] belongs to src_images[k]). */
@@ -368,6 +374,11 @@ RECON_API recon_status recon_mvs_job_recover_poses(void* ctx, int32_t job, int32
                                                    const int32_t* py, const double* depth, const double* angles,
                                                    int32_t iterations, recon_pose* out_src_poses,
                                                    double* out_cost);
+/* BgraToGray (orchestrator.cpp:53-67) on the device: w x h gray bytes,
+ * bit-identical to the reference's integer formula. */
+RECON_API recon_status recon_mvs_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride,
+                                              uint8_t* out);
+
 /* ---- the MVS stage over a capture (Orchestrator::StageMvs) ---- */
 
 typedef int32_t (*recon_mvs_cancel_fn)(void* user);              /* nonzero: cancel */
@@ -378,6 +389,8 @@ typedef struct recon_mvs_stage_params {
   int32_t batch_size;             /* maps per batched run; 0 = every map in one batch */
   int32_t consistency_views;      /* 0 = fuse every map as StageMvs does; n > 0 = fuse only pixels
                                      consistent with >= n other maps */
+  int32_t plane_normals;          /* plane mode: 1 = fused normals from the plane hypotheses; 0 = the
+                                     reference's -ray direction (FuseDepthMaps, bit-identical) */
   float consistency_rel_depth;    /* |z_back - z| / z bound of the consistency test */
   float consistency_reproj_px;    /* reprojection bound of the consistency test, pixels */
   recon_mvs_cancel_fn cancel;     /* optional, checked before every batch */

@@ -1711,3 +1711,16 @@ uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t
   free(T.support);
   return filled;
 }
+
+/* ------------------------------------------------------------------------ */
+/* BgraToGray (core/src/orchestrator/orchestrator.cpp:53-67)                */
+/* ------------------------------------------------------------------------ */
+void orc_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride, uint8_t* out) {
+  for (int y = 0; y < h; ++y) {
+    const uint8_t* row = bgra + (size_t)y * stride;
+    for (int x = 0; x < w; ++x) {
+      const int b = row[x * 4 + 0], g = row[x * 4 + 1], r = row[x * 4 + 2];
+      out[(size_t)y * w + x] = (uint8_t)((77 * r + 150 * g + 29 * b) >> 8);
+    }
+  }
+}

@@ -248,6 +248,9 @@ void orc_relative_transform_f32(const orc_pose* ref, const orc_pose* src, float 
 void orc_undistort(const uint8_t* img, int32_t w, int32_t h, const orc_intrinsics* k,
                    float* out);
 
+/* BgraToGray (orchestrator.cpp:53-67): BT.601 integer weights. */
+void orc_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -236,6 +236,8 @@ def load(which: str = "oracle") -> "Checker":
         lib.orc_plane_patchmatch.restype = C.c_uint32
         lib.orc_plane_patchmatch.argtypes = [V, P, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_float),
                                              C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.orc_bgra_to_gray.argtypes = [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
+                                         C.POINTER(C.c_uint8)]
         lib.orc_xorshift_next.restype = C.c_uint32
         lib.orc_xorshift_next.argtypes = [C.POINTER(C.c_uint64)]
         lib.orc_apply_distortion.argtypes = [C.POINTER(Intrinsics), C.c_double, C.c_double, d, d]
@@ -401,6 +403,13 @@ class Checker:
                                                _ptr(depth, C.c_float), _ptr(normal, C.c_float),
                                                _ptr(cost, C.c_float))
         return int(filled), depth, normal, cost
+
+    def bgra_to_gray(self, bgra):
+        b = np.ascontiguousarray(bgra, np.uint8)
+        h, w = b.shape[0], b.shape[1]
+        out = np.zeros((h, w), np.uint8)
+        self.lib.orc_bgra_to_gray(_ptr(b, C.c_uint8), w, h, b.strides[0], _ptr(out, C.c_uint8))
+        return out
 
     def undistort(self, img, intr):
         img = np.ascontiguousarray(img, np.uint8)

@@ -431,10 +431,20 @@ static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32,
 
 // Upload an 8-bit host image (optionally undistorted) to a device buffer;
 // returns a device pointer to either u8 or f32 data (is_f32 set).
+// An 8-bit image already on the device: undistortion (when `und` has
+// distortion) and the optional pre-filter.  Returns the image to stage.
+static const void* prepare_image(Context& C, int w, int h, const recon_camera_intrinsics* und, DevArray<uint8_t>& u8,
+                                 DevArray<float>& f32, bool* is_f32);
+
 static const void* upload_image(Context& C, const uint8_t* host, int w, int h, const recon_camera_intrinsics* und,
                                 DevArray<uint8_t>& u8, DevArray<float>& f32, bool* is_f32) {
   u8.alloc((size_t)w * h);
   CK(cudaMemcpyAsync(u8.p, host, (size_t)w * h, cudaMemcpyHostToDevice, C.stream));
+  return prepare_image(C, w, h, und, u8, f32, is_f32);
+}
+
+static const void* prepare_image(Context& C, int w, int h, const recon_camera_intrinsics* und, DevArray<uint8_t>& u8,
+                                 DevArray<float>& f32, bool* is_f32) {
   const void* out = u8.p;
   *is_f32 = false;
   if (und && distorted(*und)) {
@@ -502,6 +512,28 @@ static std::shared_ptr<StagedImage> stage_image(Context& C, const uint8_t* host,
   I->h = h;
   I->intr = k;
   upload_image(C, host, w, h, undistort ? &k : nullptr, I->u8, I->f32, &I->is_f32);
+  if (undistort) zero_distortion(&I->intr);
+  return I;
+}
+
+// A BGRA8 frame (rows `stride` bytes apart) converted to gray on the device
+// with BgraToGray's integer weights (orchestrator.cpp:53-67), then staged as
+// stage_image does.
+static std::shared_ptr<StagedImage> stage_image_bgra(Context& C, const uint8_t* bgra, int w, int h, int stride,
+                                                     const recon_camera_intrinsics& k, bool undistort) {
+  if (!bgra || w <= 0 || h <= 0 || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "BGRA image NULL, empty or short rows");
+  auto I = std::make_shared<StagedImage>();
+  I->w = w;
+  I->h = h;
+  I->intr = k;
+  DevArray<uint8_t> dev;
+  dev.alloc((size_t)4 * w * h);
+  CK(cudaMemcpy2DAsync(dev.p, (size_t)4 * w, bgra, (size_t)stride, (size_t)4 * w, h, cudaMemcpyHostToDevice,
+                       C.stream));
+  I->u8.alloc((size_t)w * h);
+  CK(launch_bgra_to_gray(dev.p, w, h, I->u8.p, C.stream));
+  prepare_image(C, w, h, undistort ? &k : nullptr, I->u8, I->f32, &I->is_f32);
+  CK(cudaStreamSynchronize(C.stream));  // the BGRA staging buffer is freed on return
   if (undistort) zero_distortion(&I->intr);
   return I;
 }
@@ -1905,9 +1937,11 @@ RECON_API void recon_mvs_point_cloud_free(recon_mvs_point_cloud* c) {
 }
 
 static FuseMap fuse_map(int w, int h, const float* depth, const uint8_t* support, const float* conf,
-                        const uint8_t* keep, const recon_camera_intrinsics& k, const recon_pose& pose) {
+                        const uint8_t* keep, const recon_camera_intrinsics& k, const recon_pose& pose,
+                        const float* normal = nullptr) {
   FuseMap M;
   std::memset(&M, 0, sizeof(M));
+  M.normal = normal;
   M.w = w;
   M.h = h;
   M.depth = depth;
@@ -2133,6 +2167,37 @@ RECON_API recon_status recon_mvs_image_stage(void* ctx, const uint8_t* gray, int
   });
 }
 
+RECON_API recon_status recon_mvs_image_stage_bgra(void* ctx, const uint8_t* bgra, int32_t w, int32_t h,
+                                                  int32_t stride, const recon_camera_intrinsics* intr,
+                                                  int32_t undistort, int32_t* out_image) {
+  return guard([&] {
+    if (!ctx || !intr || !out_image) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    Context& C = *static_cast<Context*>(ctx);
+    C.use();
+    auto I = stage_image_bgra(C, bgra, w, h, stride, *intr, undistort != 0);
+    const int id = C.next_image++;
+    C.images[id] = std::move(I);
+    *out_image = id;
+  });
+}
+
+RECON_API recon_status recon_mvs_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride,
+                                              uint8_t* out) {
+  return guard([&] {
+    if (!bgra || !out || w <= 0 || h <= 0 || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    Context& C = default_context(nullptr);
+    C.use();
+    DevArray<uint8_t> dev, g;
+    dev.alloc((size_t)4 * w * h);
+    g.alloc((size_t)w * h);
+    CK(cudaMemcpy2DAsync(dev.p, (size_t)4 * w, bgra, (size_t)stride, (size_t)4 * w, h, cudaMemcpyHostToDevice,
+                         C.stream));
+    CK(launch_bgra_to_gray(dev.p, w, h, g.p, C.stream));
+    CK(cudaMemcpyAsync(out, g.p, (size_t)w * h, cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  });
+}
+
 RECON_API recon_status recon_mvs_image_release(void* ctx, int32_t image) {
   return guard([&] {
     if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
@@ -2291,8 +2356,9 @@ RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray
     for (size_t i = 0; i < produced.size(); ++i) {
       const JobData& D = get_job(C, jobs.ids[produced[i]]);
       const int r = ref_of[produced[i]];
+      const float* nrm = (P.plane_normals && !compat) ? D.out_normal.p : nullptr;
       fm.push_back(fuse_map(D.w, D.h, D.out_depth.p, D.out_support.p, D.out_conf.p, keep[i] ? keep[i]->p : nullptr,
-                            img[r]->intr, poses[r]));
+                            img[r]->intr, poses[r], nrm));
     }
     fuse_maps(C, fm, *cfg, out_cloud);
     if (out_maps) *out_maps = (int32_t)produced.size();

@@ -38,6 +38,21 @@ __device__ __forceinline__ double norm3_d(const double* v) {
 }
 
 // Phase 1: per pixel of map m, the reference's filters and FP64 point.
+// BgraToGray (orchestrator.cpp:53-67): (77 R + 150 G + 29 B) >> 8, integer.
+__global__ void k_bgra_to_gray(const uint8_t* __restrict__ bgra, int w, int h, uint8_t* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const uchar4 p = reinterpret_cast<const uchar4*>(bgra)[(size_t)y * w + x];
+  out[(size_t)y * w + x] = (uint8_t)((77 * (int)p.z + 150 * (int)p.y + 29 * (int)p.x) >> 8);
+}
+
+cudaError_t launch_bgra_to_gray(const uint8_t* bgra, int w, int h, uint8_t* out, cudaStream_t st) {
+  const dim3 b(32, 8);
+  k_bgra_to_gray<<<dim3((w + 31) / 32, (h + 7) / 8), b, 0, st>>>(bgra, w, h, out);
+  return cudaGetLastError();
+}
+
 __global__ void k_fuse_points(FuseMap M, int64_t base, FuseParams P, unsigned long long* key, double* pos,
                               double* nrm, float* confv, uint8_t* valid) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -65,10 +80,18 @@ __global__ void k_fuse_points(FuseMap M, int64_t base, FuseParams P, unsigned lo
   double pc[3], pw[3], nr[3];
   for (int i = 0; i < 3; ++i) pc[i] = __dsub_rn(__dmul_rn(ray[i], d), M.t[i]);
   mat_t_vec_d(M.R, pc, pw);
-  mat_t_vec_d(M.R, ray, nr);
-  const double nn = norm3_d(nr);
   double nw[3];
-  for (int i = 0; i < 3; ++i) nw[i] = nn < 1e-15 ? 0.0 : __ddiv_rn(nr[i], nn);
+  if (M.normal) {
+    // the pixel's plane normal (camera frame, facing the camera) to world
+    const double nc[3] = {(double)M.normal[3 * idx], (double)M.normal[3 * idx + 1], (double)M.normal[3 * idx + 2]};
+    mat_t_vec_d(M.R, nc, nr);
+    const double nn = norm3_d(nr);
+    for (int i = 0; i < 3; ++i) nw[i] = nn < 1e-15 ? 0.0 : -__ddiv_rn(nr[i], nn);  // negated below
+  } else {
+    mat_t_vec_d(M.R, ray, nr);
+    const double nn = norm3_d(nr);
+    for (int i = 0; i < 3; ++i) nw[i] = nn < 1e-15 ? 0.0 : __ddiv_rn(nr[i], nn);
+  }
   const long long vx = (long long)floor(__ddiv_rn(pw[0], P.voxel));
   const long long vy = (long long)floor(__ddiv_rn(pw[1], P.voxel));
   const long long vz = (long long)floor(__ddiv_rn(pw[2], P.voxel));

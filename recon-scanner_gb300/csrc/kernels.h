@@ -18,6 +18,7 @@ struct FuseMap {
   const uint8_t* support;
   const float* conf;
   const uint8_t* keep;  // optional consistency mask
+  const float* normal;  // optional camera-frame unit normals (3 per pixel): fused instead of -ray
   double fx, fy, cx, cy, k1, k2, k3, p1, p2;
   double R[9], t[3];
 };
@@ -108,6 +109,7 @@ cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t 
                             cudaStream_t st);
 cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                                   cudaStream_t st);
+cudaError_t launch_bgra_to_gray(const uint8_t* bgra, int w, int h, uint8_t* out, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, int pitch, float* out, cudaStream_t st);
 cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);
 cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,

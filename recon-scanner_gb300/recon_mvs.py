@@ -130,7 +130,8 @@ PROGRESS_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double)
 
 class StageParams(C.Structure):
     _fields_ = [("undistort", C.c_int32), ("batch_size", C.c_int32), ("consistency_views", C.c_int32),
-                ("consistency_rel_depth", C.c_float), ("consistency_reproj_px", C.c_float),
+                ("plane_normals", C.c_int32), ("consistency_rel_depth", C.c_float),
+                ("consistency_reproj_px", C.c_float),
                 ("cancel", CANCEL_FN), ("progress", PROGRESS_FN), ("user", C.c_void_p)]
 
 
@@ -187,6 +188,10 @@ _SIGS = {
     "recon_mvs_image_stage": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32,
                                         C.POINTER(Intrinsics), C.c_int32, C.POINTER(C.c_int32)]),
     "recon_mvs_image_release": (C.c_int, [C.c_void_p, C.c_int32]),
+    "recon_mvs_image_stage_bgra": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
+                                             C.POINTER(Intrinsics), C.c_int32, C.POINTER(C.c_int32)]),
+    "recon_mvs_bgra_to_gray": (C.c_int, [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
+                                         C.POINTER(C.c_uint8)]),
     "recon_mvs_job_stage_images": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                              C.POINTER(Pose), C.POINTER(Pose), C.POINTER(MvsConfig),
                                              C.POINTER(C.c_int32)]),
@@ -467,6 +472,15 @@ def GeometricConsistency(depth_maps, poses, intrinsics_list, ref_index, rel_dept
     return cnt, keep
 
 
+def BgraToGray(bgra):
+    """BgraToGray (orchestrator.cpp:53-67) on the device: H x W x 4 -> H x W."""
+    b = np.ascontiguousarray(bgra, np.uint8)
+    h, w = b.shape[0], b.shape[1]
+    out = np.zeros((h, w), np.uint8)
+    _check(_lib().recon_mvs_bgra_to_gray(_ptr(b, C.c_uint8), w, h, b.strides[0], _ptr(out, C.c_uint8)))
+    return out
+
+
 def Undistort(img, intrinsics_):
     img = np.ascontiguousarray(img, np.uint8)
     out = np.zeros(img.shape, np.float32)
@@ -522,6 +536,18 @@ class Engine:
         self._img_shape[out.value] = g.shape
         return out.value
 
+    def stage_image_bgra(self, bgra, intr, undistort=False) -> int:
+        """Upload a BGRA8 frame (H x W x 4, or H x stride rows); gray on the device."""
+        b = np.ascontiguousarray(bgra, np.uint8)
+        h, w = b.shape[0], b.shape[1]
+        stride = b.strides[0]
+        k = intrinsics(intr)
+        out = C.c_int32()
+        _check(_lib().recon_mvs_image_stage_bgra(self.ctx, _ptr(b, C.c_uint8), w, h, stride, C.byref(k),
+                                                 int(undistort), C.byref(out)))
+        self._img_shape[out.value] = (h, w)
+        return out.value
+
     def release_image(self, image: int):
         _check(_lib().recon_mvs_image_release(self.ctx, image))
 
@@ -574,7 +600,8 @@ class Engine:
         return out, hist
 
     def stage_run(self, images, poses, intrinsics_list, config: MvsConfig, undistort=False, batch_size=0,
-                  consistency_views=0, rel_depth=0.01, reproj_px=1.0, cancel=None, progress=None):
+                  consistency_views=0, rel_depth=0.01, reproj_px=1.0, cancel=None, progress=None,
+                  plane_normals=False):
         """Orchestrator::StageMvs on the batched engine: keyframe images (None
         = no image), poses and intrinsics -> (PointCloud, maps fused).
         cancel() -> bool and progress(fraction) are optional callables."""
@@ -587,8 +614,8 @@ class Engine:
         ks = (Intrinsics * max(1, n))(*[intrinsics(k) for k in intrinsics_list])
         cb_cancel = CANCEL_FN((lambda _u: 1 if cancel() else 0) if cancel else 0)
         cb_progress = PROGRESS_FN((lambda _u, f: progress(f)) if progress else 0)
-        prm = StageParams(int(undistort), int(batch_size), int(consistency_views), rel_depth, reproj_px,
-                          cb_cancel, cb_progress, None)
+        prm = StageParams(int(undistort), int(batch_size), int(consistency_views), int(plane_normals), rel_depth,
+                          reproj_px, cb_cancel, cb_progress, None)
         pc = PointCloudC()
         maps = C.c_int32()
         _check(_lib().recon_mvs_stage_run(self.ctx, C.cast(ptrs, C.POINTER(C.POINTER(C.c_uint8))),

@@ -107,3 +107,59 @@ def test_stage_run_cancel_and_no_depth(mvs, capture):
     cloud, n = eng.stage_run(imgs, poses, intr, cfg)
     eng.close()
     assert n > 0 and cloud.size() > 0
+
+
+def test_stage_run_plane_normals(mvs, capture):
+    """Fused normals from the plane hypotheses: same points, and on the
+    table (world z = 0, away from the objects) they point along +z where the
+    reference's -ray normals follow the viewing directions."""
+    cams = [v.camera for v in capture.views]
+    args = ([v.image for v in capture.views], [c.pose_array() for c in cams], [c.intrinsics_array() for c in cams],
+            cfg_of(mvs, capture))
+    eng = mvs.Engine(mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0))
+    ray, _ = eng.stage_run(*args)
+    pln, _ = eng.stage_run(*args, plane_normals=True)
+    eng.close()
+    np.testing.assert_array_equal(pln.keys, ray.keys)
+    np.testing.assert_array_equal(pln.positions, ray.positions)
+    p = pln.positions
+    table = (np.abs(p[:, 2]) < 0.001) & (np.hypot(p[:, 0], p[:, 1]) > 0.14)
+    ang = lambda n: np.degrees(np.arccos(np.clip(n[table] @ np.array([0.0, 0.0, 1.0]), -1, 1)))
+    a_pln, a_ray = np.median(ang(pln.normals)), np.median(ang(ray.normals))
+    print("table points", table.sum(), "median angle to +z: plane", a_pln, "ray", a_ray)
+    assert table.sum() > 100
+    assert a_pln < 5.0 and a_pln < 0.5 * a_ray
+
+
+def test_bgra_frames(mvs, orc, capture):
+    """BgraToGray on the device is bit-identical to the oracle's restatement
+    of orchestrator.cpp:53-67 (padded rows included), and a job staged from
+    BGRA frames equals the job staged from the host-converted gray images."""
+    rng = np.random.default_rng(5)
+    frame = rng.integers(0, 256, (37, 53, 4), dtype=np.uint8)
+    padded = np.zeros((37, 60, 4), np.uint8)
+    padded[:, :53] = frame
+    assert np.array_equal(mvs.BgraToGray(padded[:, :53]), orc.bgra_to_gray(padded[:, :53]))
+    assert np.array_equal(mvs.BgraToGray(frame), orc.bgra_to_gray(frame))
+
+    cams = [v.camera for v in capture.views]
+    # colour frames whose gray image is exactly the capture's image
+    bgra = []
+    for v in capture.views:
+        g = v.image.astype(np.int32)
+        f = np.stack([g, g, g, np.full_like(g, 255)], -1).astype(np.uint8)
+        assert np.array_equal(orc.bgra_to_gray(f), (g * 256 >> 8).astype(np.uint8))
+        bgra.append(f)
+    cfg = cfg_of(mvs, capture)
+    opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0)
+    maps = []
+    for use_bgra in (False, True):
+        eng = mvs.Engine(opts)
+        ids = [eng.stage_image_bgra(f, c.intrinsics_array()) if use_bgra else
+               eng.stage_image(orc.bgra_to_gray(f), c.intrinsics_array()) for f, c in zip(bgra, cams)]
+        j = eng.stage_images(ids[0], ids[1:], cams[0].pose_array(), [c.pose_array() for c in cams[1:]], cfg)
+        eng.run(j)
+        maps.append(eng.download(j))
+        eng.close()
+    np.testing.assert_array_equal(maps[0].depth, maps[1].depth)
+    np.testing.assert_array_equal(maps[0].cost, maps[1].cost)
