@@ -64,7 +64,8 @@ struct ViewMom {
   bool valid;
 };
 
-// One view's geometry at a hypothesis: the window centre projected in FP64
+// One view's geometry at a hypothesis: the window centre projected in
+// float-float
 // (index coordinates split into an integer texel and an FP32 fraction) and
 // the FP32 transform for the offsets.  Samples are placed as centre +
 // offset, the offset computed in FP32 from differences of small quantities,
@@ -80,27 +81,36 @@ struct ViewGeo {
 __device__ __forceinline__ ViewGeo view_geo(const Job& J, const SrcView& S, const AdjHyp& h) {
   ViewGeo g;
 #pragma unroll
-  for (int i = 0; i < 9; ++i) g.A[i] = (float)S.A[i];
-  const double d = (double)h.d;
-  const double qx = ((double)h.x + 0.5 - J.drcx) / J.drfx, qy = ((double)h.y + 0.5 - J.drcy) / J.drfy;
-  const double X[3] = {qx * d, qy * d, d};
-  double Y[3];
+  for (int i = 0; i < 9; ++i) g.A[i] = S.Aff[i].hi;
+  // the window centre in float-float: X = q_c d, Y = A X + b, (u, v)
+  const ff d = ff_make(h.d);
+  const ff qx = ff_div(ff_add(ff_make((float)h.x + 0.5f), ff{-J.ffrcx.hi, -J.ffrcx.lo}), J.ffrx);
+  const ff qy = ff_div(ff_add(ff_make((float)h.y + 0.5f), ff{-J.ffrcy.hi, -J.ffrcy.lo}), J.ffry);
+  const ff X[3] = {ff_mul(qx, d), ff_mul(qy, d), d};
+  ff Y[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) Y[i] = S.A[i * 3] * X[0] + S.A[i * 3 + 1] * X[1] + S.A[i * 3 + 2] * X[2] + S.bd[i];
-  g.ok = Y[2] > 1e-6;
-  const double fx = (double)S.ffx.hi + (double)S.ffx.lo, fy = (double)S.ffy.hi + (double)S.ffy.lo;
-  const double cx = (double)S.fcx.hi + (double)S.fcx.lo, cy = (double)S.fcy.hi + (double)S.fcy.lo;
-  const double u = g.ok ? fx * (Y[0] / Y[2]) + cx - 0.5 : 0.0;
-  const double v = g.ok ? fy * (Y[1] / Y[2]) + cy - 0.5 : 0.0;
-  const double fl_u = floor(u), fl_v = floor(v);
-  const bool in_range = fabs(fl_u) < 1e8 && fabs(fl_v) < 1e8;
-  g.ok = g.ok && in_range;
-  g.iu = in_range ? (int)fl_u : 0;
-  g.iv = in_range ? (int)fl_v : 0;
-  g.fu = (float)(u - fl_u);
-  g.fv = (float)(v - fl_v);
+  for (int i = 0; i < 3; ++i)
+    Y[i] = ff_add(ff_add(ff_add(ff_mul(S.Aff[3 * i], X[0]), ff_mul(S.Aff[3 * i + 1], X[1])),
+                         ff_mul(S.Aff[3 * i + 2], X[2])),
+                  S.bff[i]);
+  g.ok = Y[2].hi > 1e-6f;
+  int iu = 0, iv = 0;
+  float fu = 0.f, fv = 0.f;
+  if (g.ok) {
+    const ff u = ff_add(ff_mul(S.ffx, ff_div(Y[0], Y[2])), ff_add(S.fcx, ff_make(-0.5f)));
+    const ff v = ff_add(ff_mul(S.ffy, ff_div(Y[1], Y[2])), ff_add(S.fcy, ff_make(-0.5f)));
+    g.ok = fabsf(u.hi) < 1e7f && fabsf(v.hi) < 1e7f;
+    if (g.ok) {
+      ff_floor_frac(u, &iu, &fu);
+      ff_floor_frac(v, &iv, &fv);
+    }
+  }
+  g.iu = iu;
+  g.iv = iv;
+  g.fu = fu;
+  g.fv = fv;
 #pragma unroll
-  for (int i = 0; i < 3; ++i) g.Yc[i] = (float)Y[i];
+  for (int i = 0; i < 3; ++i) g.Yc[i] = __fadd_rn(Y[i].hi, Y[i].lo);
   return g;
 }
 

@@ -150,6 +150,7 @@ struct SrcView {
   ff bff[3];
   double A[9];
   double bd[3];
+  ff Aff[9];  // A in float-float (per-pixel source rays without FP64)
 };
 
 // Columns of one reference-tile plane staged by a sweep block: the warp's 32
@@ -166,6 +167,7 @@ struct Job {
   int min_valid;  // patch_size * patch_size / 2 (patchmatch_stereo.cpp:245)
   float rfx, rfy, rcx, rcy;
   double drfx, drfy, drcx, drcy;
+  ff ffrx, ffry, ffrcx, ffrcy;  // the same in float-float
   int ref_distorted;
   double rk1, rk2, rk3, rp1, rp2;
   const float* ref;      // (I - 128), row-major w x h

@@ -492,7 +492,10 @@ static void set_src_transform(SrcView& S, const recon_pose& ref, const recon_pos
                               const recon_camera_intrinsics& rk) {
   double A[9], b[3];
   relative_transform(ref, src, A, b);
-  for (int i = 0; i < 9; ++i) S.A[i] = A[i];
+  for (int i = 0; i < 9; ++i) {
+    S.A[i] = A[i];
+    S.Aff[i] = ff_host(A[i]);
+  }
   for (int i = 0; i < 3; ++i) {
     S.bd[i] = b[i];
     S.b[i] = (float)b[i];
@@ -656,6 +659,10 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
   J.drfy = rk.fy;
   J.drcx = rk.cx;
   J.drcy = rk.cy;
+  J.ffrx = ff_host(rk.fx);
+  J.ffry = ff_host(rk.fy);
+  J.ffrcx = ff_host(rk.cx);
+  J.ffrcy = ff_host(rk.cy);
   J.ref_distorted = distorted(rk) ? 1 : 0;
   J.rk1 = rk.k1;
   J.rk2 = rk.k2;

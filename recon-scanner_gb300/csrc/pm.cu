@@ -45,6 +45,23 @@ struct PCache {
 };
 
 __device__ __forceinline__ void fill_pcache(const Job& J, const PCache& pc, int x, int y, float* rx, float* ry) {
+  if (J.hyp && !J.ref_distorted) {
+    // plane mode, pinhole reference: the pixel ray and P_s = A_s ray in
+    // float-float (~44-bit mantissa) -- no FP64 on the device, whose rate on
+    // this part is 1/64 of FP32
+    const ff xr = ff_div(ff_add(ff_make((float)x + 0.5f), ff{-J.ffrcx.hi, -J.ffrcx.lo}), J.ffrx);
+    const ff yr = ff_div(ff_add(ff_make((float)y + 0.5f), ff{-J.ffrcy.hi, -J.ffrcy.lo}), J.ffry);
+    for (int s = 0; s < J.num_src; ++s) {
+      const SrcView& S = J.src[s];
+      ff P[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) P[i] = ff_add(ff_add(ff_mul(S.Aff[3 * i], xr), ff_mul(S.Aff[3 * i + 1], yr)), S.Aff[3 * i + 2]);
+      pc.put(s, P);
+    }
+    *rx = __fadd_rn(xr.hi, xr.lo);
+    *ry = __fadd_rn(yr.hi, yr.lo);
+    return;
+  }
   double ray[3];
   ref_ray(J, x + 0.5, y + 0.5, ray);
   for (int s = 0; s < J.num_src; ++s) {
