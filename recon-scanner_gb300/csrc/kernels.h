@@ -111,7 +111,6 @@ cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, siz
                                   cudaStream_t st);
 cudaError_t launch_bgra_to_gray(const uint8_t* bgra, int w, int h, uint8_t* out, cudaStream_t st);
 cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, int pitch, float* out, cudaStream_t st);
-cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st);
 cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const uint8_t* src, int src_w, int src_h,
                                int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,
                                int* samples, cudaStream_t st);

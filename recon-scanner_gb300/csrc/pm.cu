@@ -1142,9 +1142,6 @@ __global__ void k_ncc_windows(const uint8_t* __restrict__ ref, int ref_w, int re
   samples_out[i] = ok ? valid : 0;
 }
 
-__global__ void k_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out) {
-  *out = tex2Dgather<float4>(tex, x, y, 0);
-}
 
 // ---------------------------------------------------------------------------
 // host launchers
@@ -1340,9 +1337,5 @@ cudaError_t launch_deinterleave(const float* ref, int w, int h, int half_w, int 
   return cudaGetLastError();
 }
 
-cudaError_t launch_gather_probe(cudaTextureObject_t tex, float x, float y, float4* out, cudaStream_t st) {
-  k_gather_probe<<<1, 1, 0, st>>>(tex, x, y, out);
-  return cudaGetLastError();
-}
 
 }  // namespace rmvs
