@@ -73,6 +73,7 @@ struct ViewMom {
 struct ViewGeo {
   float A[9];
   float Yc[3];    // window-centre point, source camera
+  float izc;      // 1 / Yc.z
   int iu, iv;     // texel of the centre (index coordinate = coordinate - 0.5)
   float fu, fv;   // its fraction
   bool ok;        // centre in front of the source (the search's rule)
@@ -111,6 +112,7 @@ __device__ __forceinline__ ViewGeo view_geo(const Job& J, const SrcView& S, cons
   g.fv = fv;
 #pragma unroll
   for (int i = 0; i < 3; ++i) g.Yc[i] = __fadd_rn(Y[i].hi, Y[i].lo);
+  g.izc = 1.0f / g.Yc[2];
   return g;
 }
 
@@ -128,7 +130,7 @@ __device__ __forceinline__ bool adj_sample(const Job& J, const SrcView& S, const
   const float m = h.kappa + ndq;
   if (!(m < 0.0f)) return false;
   // X_k - X_c = d (kappa dq - (n . dq) q_c) / m_k   (exact small quantities)
-  const float sc = h.d / m;
+  const float sc = h.d * rcp_approx(m);
   const float dX[3] = {sc * (h.kappa * dq0 - ndq * h.qc[0]), sc * (h.kappa * dq1 - ndq * h.qc[1]), -sc * ndq};
   float dY[3];
 #pragma unroll
@@ -139,8 +141,8 @@ __device__ __forceinline__ bool adj_sample(const Job& J, const SrcView& S, const
     X[i] = h.d * h.qc[i] + dX[i];
   }
   if (!(Y[2] > 1e-9f)) return false;
-  const float iz = 1.0f / Y[2];
-  const float izc = 1.0f / geo.Yc[2];
+  const float iz = rcp_approx(Y[2]);
+  const float izc = geo.izc;
   // offset from the centre in index coordinates
   const float du = S.fx * (dY[0] * geo.Yc[2] - geo.Yc[0] * dY[2]) * (iz * izc);
   const float dv = S.fy * (dY[1] * geo.Yc[2] - geo.Yc[1] * dY[2]) * (iz * izc);
@@ -370,6 +372,30 @@ __device__ int plane_adjoint(const Job& J, const AdjHyp& h, float* cost, float g
       for (int i = 0; i < 6; ++i) pose_grad[6 * s + i] = gp[i] * inv_k;
   }
   return k;
+}
+
+// The gradient and Gauss-Newton matrix of the mean cost of the views in
+// `sel` (a bit per source, k of them, chosen by the caller -- the best_k of
+// the search's own evaluation): per view one moments pass and one adjoint
+// pass, nothing kept per view.  Returns false if a selected view turns
+// invalid under the exact reads.
+template <int kMode>
+__device__ bool plane_adjoint_selected(const Job& J, const AdjHyp& h, uint32_t sel, int k, float g[3], float H[6]) {
+  for (int i = 0; i < 3; ++i) g[i] = 0.f;
+  for (int i = 0; i < 6; ++i) H[i] = 0.f;
+  if (k <= 0) return false;
+  const float inv_k = 1.0f / (float)k;
+  for (int s = 0; s < J.num_src; ++s) {
+    if (!((sel >> s) & 1u)) continue;
+    const ViewGeo geo = view_geo(J, J.src[s], h);
+    const ViewMom mo = view_moments<kMode>(J, J.src[s], geo, h);
+    if (!mo.valid) return false;
+    float gs[3], Hs[6];
+    view_adjoint<kMode, false>(J, J.src[s], geo, h, mo, gs, Hs, nullptr, nullptr);
+    for (int i = 0; i < 3; ++i) g[i] += gs[i] * inv_k;
+    for (int i = 0; i < 6; ++i) H[i] += Hs[i] * inv_k;
+  }
+  return true;
 }
 
 // Solves (H + lambda diag(H)) x = -g for the symmetric 3 x 3 H (upper
