@@ -421,6 +421,30 @@ def fuse_capture(M, scenes, maps, rel=0.01, reproj=1.0, min_views=3):
             "timing": "host wall clock: 9 consistency calls + fusion, host buffers in and out"}
 
 
+def reference_algorithm_map(M, sc, cfg):
+    """The reference's own algorithm on one map of the workload:
+    PatchMatchStereo + RefineSubpixel (fronto-parallel windows, golden
+    section + parabola fit; patchmatch_stereo.cpp:422-979) run by the
+    engine's COMPAT mode, its device restatement, on the views undistorted on
+    the device and rounded to 8 bits (the reference's input type), with
+    pinhole cameras.  Returns its accuracy vs analytic truth and its time."""
+    import numpy as np
+
+    vs = [sc.ref] + list(sc.sources)
+    imgs = [np.clip(np.rint(M.Undistort(v.image, v.camera.intrinsics_array())), 0, 255).astype(np.uint8) for v in vs]
+    cams = [v.camera.undistorted() for v in vs]
+    va = M.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    opts = M.Options(mode=M.MODE_COMPAT, device=0)
+    t0 = time.perf_counter()
+    dm = M.PatchMatchStereo(va, cfg, options=opts)
+    M.RefineSubpixel(va, cfg, dm, options=opts)
+    secs = time.perf_counter() - t0
+    out = accuracy([dm], [sc.ref.depth])
+    out["seconds"] = secs
+    out["note"] = "map 0 only; COMPAT mode = the reference's PatchMatchStereo + RefineSubpixel restated on the device"
+    return out
+
+
 def stage_capture_run(M, scenes, opts):
     """The whole MVS stage of the capture through one public call
     (recon_mvs_stage_run: host images in, fused cloud out): staging with
@@ -578,6 +602,10 @@ def run_gpu(args):
     if WORKLOAD == "c2" and not args.no_fusion:
         line["fusion"] = fuse_capture(M, scenes, maps)
         line["stage"] = stage_capture_run(M, scenes, opts)
+    if WORKLOAD == "c2" and not args.no_reference_map:
+        ra = reference_algorithm_map(M, scenes[0], cfgs[0])
+        ra["chosen_same_map"] = accuracy(maps[:1], truths[:1])
+        line["reference_algorithm"] = ra
     if rank == 0 and not args.no_cpu_baseline:
         secs, threads, note = cpu_reference_sample(scenes[0])
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
@@ -886,6 +914,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3", "c4", "c5"])
     ap.add_argument("--no-fusion", action="store_true", help="skip the capture's consistency + fusion stage")
+    ap.add_argument("--no-reference-map", action="store_true",
+                    help="skip the reference algorithm's map (COMPAT mode) on map 0 of the capture")
     ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
     ap.add_argument("--tile-rows", type=int, default=0, help="sweep tile rows (2, 4, 8); 0 = autotuned")
     args = ap.parse_args()

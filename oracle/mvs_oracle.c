@@ -1114,6 +1114,9 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
   const double X0[3] = {r0[0] * depth, r0[1] * depth, depth};
   const double delta = n[0] * X0[0] + n[1] * X0[1] + n[2] * X0[2];
   if (!(delta < 0.0)) return res; /* plane must face the camera */
+  /* grazing planes (normal within ~3 degrees of perpendicular to the ray)
+     are not plane-mode hypotheses */
+  if (!(n[0] * r0[0] + n[1] * r0[1] + n[2] < -0.05 * sqrt(r0[0] * r0[0] + r0[1] * r0[1] + 1.0))) return res;
   const int half = cfg->patch_size / 2;
   const int min_valid = cfg->patch_size * cfg->patch_size / 2;
   double refc[3];
@@ -1454,12 +1457,9 @@ typedef struct {
   int y0, y1;
 } pm_task;
 
-static double pm_eval(const pm_task* T, int x, int y, double rx, double ry, double rho, const double n[3],
-                      int32_t* support) {
+static double pm_eval(const pm_task* T, int x, int y, double rho, const double n[3], int32_t* support) {
   *support = 0;
   if (!(rho > 0.0) || rho < T->rho_min || rho > T->rho_max) return 1e30;
-  const double kappa = n[0] * rx + n[1] * ry + n[2];
-  if (!(kappa < -0.05 * sqrt(rx * rx + ry * ry + 1.0))) return 1e30;
   const orc_plane_result r = orc_plane_cost(T->v, T->cfg, T->best_k, x, y, rho, n, 0);
   *support = r.valid_views;
   return r.cost;
@@ -1484,7 +1484,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
     double n[3];
     pm_random_normal(&g, rx, ry, n);
     int32_t sup;
-    T->cost[idx] = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+    T->cost[idx] = pm_eval(T, x, y, rho, n, &sup);
     T->support[idx] = sup;
     h[0] = rho;
     h[1] = n[0];
@@ -1530,7 +1530,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
       if (hn[1] == cur[1] && hn[2] == cur[2] && hn[3] == cur[3] && fabs(rho - cur[0]) <= 4e-6 * cur[0]) continue;
       const double n[3] = {hn[1], hn[2], hn[3]};
       int32_t sup;
-      const double c = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+      const double c = pm_eval(T, x, y, rho, n, &sup);
       if (c < cur_cost) {
         cur_cost = c;
         cur[0] = rho;
@@ -1558,7 +1558,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
         if (q & 2) pm_perturb_normal(&g, rx, ry, 0.5 * scale, n);
       }
       int32_t sup;
-      const double c = pm_eval(T, x, y, rx, ry, rho, n, &sup);
+      const double c = pm_eval(T, x, y, rho, n, &sup);
       if (c < cur_cost) {
         cur_cost = c;
         cur[0] = rho;
@@ -1585,7 +1585,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
     const double inv_phi = 0.618033988749895;
     double c1 = hi - inv_phi * (hi - lo), c2 = lo + inv_phi * (hi - lo);
     int32_t s1, s2, sm;
-    double f1 = pm_eval(T, x, y, rx, ry, c1, n, &s1), f2 = pm_eval(T, x, y, rx, ry, c2, n, &s2);
+    double f1 = pm_eval(T, x, y, c1, n, &s1), f2 = pm_eval(T, x, y, c2, n, &s2);
     for (int q = 0; q < T->cfg->subpixel_iterations; ++q) {
       if (f1 < f2) {
         hi = c2;
@@ -1593,18 +1593,18 @@ static void pm_pixel(const pm_task* T, int x, int y) {
         f2 = f1;
         s2 = s1;
         c1 = hi - inv_phi * (hi - lo);
-        f1 = pm_eval(T, x, y, rx, ry, c1, n, &s1);
+        f1 = pm_eval(T, x, y, c1, n, &s1);
       } else {
         lo = c1;
         c1 = c2;
         f1 = f2;
         s1 = s2;
         c2 = lo + inv_phi * (hi - lo);
-        f2 = pm_eval(T, x, y, rx, ry, c2, n, &s2);
+        f2 = pm_eval(T, x, y, c2, n, &s2);
       }
     }
     const double mid = 0.5 * (lo + hi);
-    const double fm = pm_eval(T, x, y, rx, ry, mid, n, &sm);
+    const double fm = pm_eval(T, x, y, mid, n, &sm);
     if (fm < best_c) {
       best_c = fm;
       best_d = mid;

@@ -105,9 +105,12 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
                                   float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
                                   int* nevals = nullptr) {
   HypCost bad{kCostInf, 0};
-  if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max) return bad;
   PlaneHyp hp;
-  if (!make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) return bad;
+  if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max || !make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) {
+    if (view_cost)
+      for (int s = 0; s < J.num_src; ++s) view_cost[s] = kCostInf;
+    return bad;
+  }
   if (nevals) ++*nevals;
   float best[kMaxBestK];
 #pragma unroll
