@@ -53,9 +53,9 @@ sys.path.insert(0, os.path.join(ROOT, "recon-scanner_gb300"))
 METRIC = "depth maps/s 1920×1440×8src (1 GB300), chosen vs plain GPU at ≤0.1% depth err"
 K, S_SRC = 11, 8
 W, H, F, ITERS = 1920, 1440, 1450.0, 8
-# per pixel-hypothesis algorithmic FLOP, plane-induced homography mode:
-# S * (K^2 * 26 + 30) + 40  (26 = 15 projection + 6 bilinear + 5 moments)
-FLOP_PER_HYP = S_SRC * (K * K * 26 + 30) + 40
+# algorithmic FLOP of the plane-induced homography cost: K^2 * 26 + 30 per
+# source window sampled (26 = 15 projection + 6 bilinear + 5 moments), 40 per
+# hypothesis
 SM_COUNT, FP32_LANES = 152, 128
 
 
@@ -136,11 +136,10 @@ def set_workload(name):
     sources sphere scene (one map; profiling captures, CPU-runnable size);
     c3: 48 references from a 120-frame orbit, mixed resolutions, 6-10
     sources each."""
-    global WORKLOAD, W, H, F, ITERS, S_SRC, FLOP_PER_HYP
+    global WORKLOAD, W, H, F, ITERS, S_SRC
     WORKLOAD = name
     if name == "small":
         W, H, F, ITERS, S_SRC = 640, 480, 600.0, 6, 4
-    FLOP_PER_HYP = S_SRC * (K * K * 26 + 30) + 40
 
 
 def views_of(M, sc):
@@ -305,7 +304,8 @@ def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, samp
     timed steps (CUDA events on the engine stream around the whole run; L2
     flushed between steps, outside the events).  A step runs every view:
     as one batch, or one launch per view when opts.per_view = 1.  Returns
-    per-step ms, sweep ms, hypotheses, launches/step, maps, stats."""
+    per-step ms, sweep ms, (hypotheses, source windows sampled) per step,
+    launches/step, maps, stats."""
     import torch
 
     eng = M.Engine(opts)
@@ -316,7 +316,7 @@ def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, samp
     for _ in range(warmup):
         eng.run_many(jobs)
         eng.synchronize()
-    step_ms, sweep_ms, hyps = [], [], []
+    step_ms, sweep_ms, hyps, wins = [], [], [], []
     launches = 0
     barrier(world)
     ctx = sampler if sampler is not None else _Null()
@@ -324,13 +324,14 @@ def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, samp
         for _ in range(steps):
             flush.random_(0, 255)
             torch.cuda.synchronize()
-            h0 = eng.stats().hypotheses_evaluated
+            s0 = eng.stats()
             eng.run_many(jobs)
             eng.synchronize()
             st = eng.stats()
             step_ms.append(st.last_run_ms)
             sweep_ms.append(st.last_sweep_ms)
-            hyps.append(st.hypotheses_evaluated - h0)
+            hyps.append(st.hypotheses_evaluated - s0.hypotheses_evaluated)
+            wins.append(st.windows_evaluated - s0.windows_evaluated)
     barrier(world)
     st = eng.stats()
     groups = len(jobs) if opts.per_view else -(-len(jobs) // 64)
@@ -339,7 +340,7 @@ def time_form(M, views, cfgs, opts, steps, warmup, flush, world, undistort, samp
     for j in jobs:
         eng.release(j)
     eng.close()
-    return step_ms, sweep_ms, hyps, launches, maps, st
+    return step_ms, sweep_ms, (hyps, wins), launches, maps, st
 
 
 class _Null:
@@ -487,7 +488,8 @@ def run_gpu(args):
     n_src = [len(sc.sources) for sc in scenes]
     # pixel-weighted sources per map: the FLOP model's S for mixed batches
     s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
-    flop_per_hyp = s_eff * (K * K * 26 + 30) + 40
+    # FLOP model: per source window sampled K*K*26 + 30, per hypothesis 40
+    flop_per_window, flop_per_hyp_setup = K * K * 26 + 30, 40
     mk = lambda fp16, interp, per_view, refine: M.Options(
         mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
         refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
@@ -496,7 +498,7 @@ def run_gpu(args):
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
     clk = ClockSampler(local)
-    step_ms, sweep_ms, hyps, launches_per_step, maps, st = time_form(M, views, cfgs, opts, args.steps, args.warmup,
+    step_ms, sweep_ms, (hyps, wins), launches_per_step, maps, st = time_form(M, views, cfgs, opts, args.steps, args.warmup,
                                                                      flush, world, undistort, clk, scenes=scenes)
     total_ms = barrier_max(world, float(sum(step_ms)))
     value = world * n_maps * args.steps / (total_ms / 1000.0)
@@ -555,15 +557,19 @@ def run_gpu(args):
     sweeps = max(1, st.last_sweep_launches)
     per_launch_ms = statistics.mean(sweep_ms) / sweeps
     hyp_per_launch = statistics.mean(hyps) / sweeps
-    achieved_tflops = flop_per_hyp * hyp_per_launch / (per_launch_ms * 1e-3) / 1e12
+    win_per_launch = statistics.mean(wins) / sweeps
+    flop_per_launch = flop_per_window * win_per_launch + flop_per_hyp_setup * hyp_per_launch
+    achieved_tflops = flop_per_launch / (per_launch_ms * 1e-3) / 1e12
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     peak_tflops = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
-    traffic = None
+    traffic, tex_pipe = None, None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("plane_sweep_bytes_per_launch", {}).get(
-                f"{WORKLOAD}{'_per_view' if args.per_view else ''}")
+            prof = json.load(f)
+        key = f"{WORKLOAD}{'_per_view' if args.per_view else ''}"
+        traffic = prof.get("plane_sweep_bytes_per_launch", {}).get(key)
+        tex_pipe = prof.get("plane_sweep_tex_data_pipe_pct", {}).get(key)
 
     form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
             f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
@@ -595,8 +601,14 @@ def run_gpu(args):
                          "kernel": "k_plane_sweep",
                          "peak_source": f"{SM_COUNT} SMs x {FP32_LANES} FP32 lanes x 2 x sm_max_mhz {sm_mhz} "
                                         f"({peak_src} MEASURED_PEAKS.json clock)",
-                         "hypotheses_per_launch": hyp_per_launch, "ms_per_launch": per_launch_ms,
-                         "flop_per_hypothesis": flop_per_hyp},
+                         "hypotheses_per_launch": hyp_per_launch, "windows_per_launch": win_per_launch,
+                         "ms_per_launch": per_launch_ms, "flop_per_launch": flop_per_launch,
+                         "flop_model": f"{flop_per_window} per source window sampled + {flop_per_hyp_setup} per "
+                                       f"hypothesis",
+                         "binding_unit": {"unit": "L1TEX texture data pipe (bilinear source reads)",
+                                          "pct_of_peak": tex_pipe,
+                                          "source": "ncu l1tex__data_pipe_tex_wavefronts.avg."
+                                                    "pct_of_peak_sustained_elapsed, profiles/traffic.json"}},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
             "accuracy": acc, "plain": plain, "clocks": clk.summary()}
     if WORKLOAD == "c2" and not args.no_fusion:

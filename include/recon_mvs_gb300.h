@@ -219,6 +219,8 @@ typedef struct recon_mvs_stats {
   int32_t graph_launches;        /* CUDA-graph replays so far */
   int32_t tune_trials;           /* autotuner searches run by this context */
   int32_t reserved[1];
+  uint64_t windows_evaluated;    /* plane sweeps: source windows sampled (a hypothesis samples up to one
+                                    per source; views that cannot change its fate are skipped) */
 } recon_mvs_stats;
 
 /* ---- version and configuration ---------------------------------------- */

@@ -201,7 +201,7 @@ struct Job {
   float photo_threshold;
   int best_k;
   uint64_t seed;
-  unsigned long long* eval_counter;  // optional: hypotheses whose windows were evaluated
+  unsigned long long* eval_counter;  // optional: [0] hypotheses evaluated, [1] source windows sampled
   // plane-mode run parameters (read by the batched kernels per work item)
   const float* seed_depth;  // optional per-32-px-cell seed depth, seed_gx cells per row
   int seed_gx;

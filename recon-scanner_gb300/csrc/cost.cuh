@@ -30,7 +30,7 @@ namespace rmvs {
 
 struct ViewResult {
   float ncc;
-  int valid;
+  int valid;  // 1 valid; 0 invalid after sampling; -1 invalid before sampling (plane mode)
 };
 
 // Window moments of the reference image for one pixel (full window).
@@ -464,7 +464,7 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
 template <int H, int kMode, class Ref>
 __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
                                                       const PlaneHyp& hp, const RefWindow& rw, const Ref& ref) {
-  ViewResult bad{0.0f, 0};
+  ViewResult bad{0.0f, -1};  // nothing sampled
   ff u0, v0;
   float xz, mx, my;
   if (!source_centre(S, P, ff_make(hp.rho), hp.rho, &u0, &v0, &xz, &mx, &my)) return bad;

@@ -335,8 +335,8 @@ struct Context {
     CK(cudaEventCreate(&ev_sweep0));
     CK(cudaEventCreate(&ev_sweep1));
     CK(cudaEventCreate(&ev_end));
-    counter.alloc(1);
-    CK(cudaMemsetAsync(counter.p, 0, sizeof(unsigned long long), stream));
+    counter.alloc(2);  // hypotheses, source windows sampled
+    CK(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned long long), stream));
     err.alloc(1);
     CK(cudaMemsetAsync(err.p, 0, sizeof(int), stream));
   }
@@ -912,8 +912,8 @@ static void tune_group(Context& C, PlaneGroup& G) {
     set_shape(4, std::max(1, occupancy(4)));
     return;
   }
-  unsigned long long saved = 0;
-  CK(cudaMemcpyAsync(&saved, C.counter.p, sizeof(saved), cudaMemcpyDeviceToHost, C.stream));
+  unsigned long long saved[2] = {0, 0};
+  CK(cudaMemcpyAsync(saved, C.counter.p, sizeof(saved), cudaMemcpyDeviceToHost, C.stream));
   CK(cudaStreamSynchronize(C.stream));
   float best_ms = 1e30f;
   TuneChoice best;
@@ -937,7 +937,7 @@ static void tune_group(Context& C, PlaneGroup& G) {
       }
     }
   }
-  CK(cudaMemcpyAsync(C.counter.p, &saved, sizeof(saved), cudaMemcpyHostToDevice, C.stream));
+  CK(cudaMemcpyAsync(C.counter.p, saved, sizeof(saved), cudaMemcpyHostToDevice, C.stream));
   CK(cudaStreamSynchronize(C.stream));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1211,6 +1211,14 @@ static void check_device_error(Context& C) {
   }
 }
 
+// The evaluation counters (hypotheses, source windows sampled) into the stats.
+static void read_counters(Context& C) {
+  unsigned long long ev[2] = {0, 0};
+  CK(cudaMemcpy(ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
+  C.stats.hypotheses_evaluated = ev[0];
+  C.stats.windows_evaluated = ev[1];
+}
+
 static void finish_stats(Context& C) {
   float ms = 0.f, sw = 0.f;
   if (cudaEventElapsedTime(&ms, C.ev_start, C.ev_end) == cudaSuccess) C.stats.last_run_ms = ms;
@@ -1280,9 +1288,7 @@ static void download_job(Context& C, JobData& D, recon_mvs_depth_map* out, uint3
   CK(cudaStreamSynchronize(C.stream));
   check_device_error(C);
   finish_stats(C);
-  unsigned long long ev = 0;
-  CK(cudaMemcpy(&ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
-  C.stats.hypotheses_evaluated = ev;
+  read_counters(C);
   if (filled) *filled = f;
 }
 
@@ -2407,9 +2413,7 @@ RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out) 
     if (!ctx || !out) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
     Context& C = *static_cast<Context*>(ctx);
     C.use();
-    unsigned long long ev = 0;
-    CK(cudaMemcpy(&ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
-    C.stats.hypotheses_evaluated = ev;
+    read_counters(C);
     *out = C.stats;
   });
 }

@@ -100,10 +100,18 @@ __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int 
   return r;
 }
 
+// `beat`: the cost a candidate must get below to be taken (the caller keeps
+// it only if cost < beat).  View costs lie in [0, 2], so after each view the
+// final cost is bounded below by letting every remaining view be valid at
+// cost 0: with K = best_k (or all views), n valid so far, r views left and
+// k' = min(K, n + r), cost >= (sum of the k' - r lowest costs so far) / k'.
+// Once that bound is above `beat` (with a relative margin that covers the
+// rounding of both sums) the remaining views cannot change the decision and
+// are not evaluated: the candidate is returned as rejected.
 template <int H, int kMode, class Ref>
 __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
                                   float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
-                                  int* nevals = nullptr) {
+                                  int* counts = nullptr, float beat = kCostInf) {
   HypCost bad{kCostInf, 0};
   PlaneHyp hp;
   if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max || !make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) {
@@ -111,18 +119,26 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
       for (int s = 0; s < J.num_src; ++s) view_cost[s] = kCostInf;
     return bad;
   }
-  if (nevals) ++*nevals;
+  if (counts) ++counts[0];
   float best[kMaxBestK];
 #pragma unroll
   for (int i = 0; i < kMaxBestK; ++i) best[i] = kCostInf;
   float sum_all = 0.f;
   int nvalid = 0;
+  const bool all_views = J.best_k <= 0 || J.best_k > kMaxBestK;
+  const int K = all_views ? J.num_src : J.best_k;
+  const float bar = beat * (1.0f + 4e-6f);
+  bool pruned = false;
   for (int s = 0; s < J.num_src; ++s) {
-    ff P[3];
-    pc.get(s, P);
-    const ViewResult v = eval_view_plane<H, kMode>(J, J.src[s], x, y, P, hp, rw, ref);
+    ViewResult v{0.0f, 0};
+    if (!pruned) {
+      ff P[3];
+      pc.get(s, P);
+      v = eval_view_plane<H, kMode>(J, J.src[s], x, y, P, hp, rw, ref);
+    }
+    if (counts) counts[1] += v.valid >= 0;
     float c = kCostInf;
-    if (v.valid) {
+    if (v.valid > 0) {
       c = 1.0f - v.ncc;
       ++nvalid;
       sum_all += c;
@@ -135,7 +151,22 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
       c = 1.0f - v.ncc;
     }
     if (view_cost) view_cost[s] = c;
+    const int left = J.num_src - 1 - s;
+    if (left > 0 && left < K && nvalid > 0) {
+      const int kk = min(K, nvalid + left), j = kk - left;
+      float lb;
+      if (all_views) {
+        lb = sum_all;  // j == nvalid: every valid view so far
+      } else {
+        lb = 0.f;
+#pragma unroll
+        for (int i = 0; i < kMaxBestK; ++i)
+          if (i < j) lb += best[i];
+      }
+      pruned = pruned || (j > 0 && lb > bar * (float)kk);
+    }
   }
+  if (pruned) return HypCost{kCostInf, 0};
   return finish_plane(best, sum_all, nvalid, J.best_k, J.photo_threshold);
 }
 
@@ -391,7 +422,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
   float cur_cost = J.cost[idx];
   int cur_sup = J.support[idx];
   const float ifx = 1.0f / J.rfx, ify = 1.0f / J.rfy;
-  int nevals = 0;
+  int counts[2] = {0, 0};  // hypotheses, source windows sampled
 
   // --- propagation: best-cost neighbour of each region ---
   for (int r = 0; r < 8; ++r) {
@@ -432,7 +463,8 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     // the transfer): nothing to learn -- in a converged region most regions
     // propose exactly this
     if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) continue;
-    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, &nevals);
+    const HypCost c =
+        eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts, cur_cost);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);
@@ -459,7 +491,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
     }
-    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, &nevals);
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, counts, cur_cost);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, nx, ny, nz);
@@ -467,8 +499,13 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     }
   }
   if (J.eval_counter) {
-    const unsigned int lane_sum = __reduce_add_sync(__activemask(), (unsigned int)nevals);
-    if ((threadIdx.x & 31) == (__ffs(__activemask()) - 1)) atomicAdd(J.eval_counter, (unsigned long long)lane_sum);
+    const unsigned int m = __activemask();
+    const unsigned int hyps = __reduce_add_sync(m, (unsigned int)counts[0]);
+    const unsigned int wins = __reduce_add_sync(m, (unsigned int)counts[1]);
+    if ((threadIdx.x & 31) == (__ffs(m) - 1)) {
+      atomicAdd(J.eval_counter, (unsigned long long)hyps);
+      atomicAdd(J.eval_counter + 1, (unsigned long long)wins);
+    }
   }
   J.hyp[idx] = cur;
   J.cost[idx] = cur_cost;
@@ -996,7 +1033,8 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constan
       const float nd = d + step[0], nt = theta + step[1], np = phi + step[2];
       float n[3], dt[3], dp[3];
       sph_normal(nt, np, n, dt, dp);
-      const HypCost hc = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, 1.0f / nd, n[0], n[1], n[2], rw, ref, nullptr);
+      const HypCost hc =
+          eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, 1.0f / nd, n[0], n[1], n[2], rw, ref, nullptr, nullptr, cur);
       if (nd > 0.f && hc.cost < cur) {
         d = nd;
         theta = nt;

@@ -121,7 +121,8 @@ class PointCloudC(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("hypotheses_evaluated", C.c_uint64), ("last_run_ms", C.c_double), ("last_sweep_ms", C.c_double),
                 ("last_sweep_launches", C.c_int32), ("tile_rows", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("reserved", C.c_int32 * 1)]
+                ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("reserved", C.c_int32 * 1),
+                ("windows_evaluated", C.c_uint64)]
 
 
 CANCEL_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p)
