@@ -686,6 +686,7 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
   J.max_depth = cfg->max_depth_m;
   J.photo_threshold = (float)cfg->photo_threshold;
   J.best_k = C.opts.best_k;
+  J.prune = C.opts.exhaustive ? 0 : 1;
   J.seed = C.opts.seed;
   J.eval_counter = C.counter.p;
 

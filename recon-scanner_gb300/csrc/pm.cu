@@ -130,7 +130,7 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
   const float bar = beat * (1.0f + 4e-6f);
   bool pruned = false;
   for (int s = 0; s < J.num_src; ++s) {
-    ViewResult v{0.0f, 0};
+    ViewResult v{0.0f, -1};  // skipped: not sampled
     if (!pruned) {
       ff P[3];
       pc.get(s, P);
@@ -464,7 +464,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     // propose exactly this
     if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) continue;
     const HypCost c =
-        eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts, cur_cost);
+        eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts, J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);
@@ -491,7 +491,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
       if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
       if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
     }
-    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, counts, cur_cost);
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, counts, J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, nx, ny, nz);
@@ -1034,7 +1034,8 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constan
       float n[3], dt[3], dp[3];
       sph_normal(nt, np, n, dt, dp);
       const HypCost hc =
-          eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, 1.0f / nd, n[0], n[1], n[2], rw, ref, nullptr, nullptr, cur);
+          eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, 1.0f / nd, n[0], n[1], n[2], rw, ref, nullptr, nullptr,
+                                   J.prune ? cur : kCostInf);
       if (nd > 0.f && hc.cost < cur) {
         d = nd;
         theta = nt;

@@ -5,6 +5,8 @@ bit-identical maps: images smaller than a tile or a window, a degenerate job
 (zero baseline) inside a batch, a job with zero iterations, mixed window
 sizes (two groups in one plan), 32 sources (the maximum; per-thread ray cache
 above 48 KB of shared memory), Gauss-Newton refinement on BF16 storage.
+The sweep's exact view pruning is checked the same way: with and without it
+the maps are bit-identical while fewer source windows are sampled.
 """
 import numpy as np
 import pytest
@@ -110,3 +112,31 @@ def test_gauss_newton_on_bf16(mvs):
     same(a, b)
     err = np.abs(a[0].depth - sc.ref.depth)[8:-8, 8:-8]
     assert np.nanmedian(err) < 2e-3
+
+
+@pytest.mark.parametrize("best_k,refine,interp", [(3, 2, 1), (0, 1, 0), (8, 2, 0), (4, 1, 1)])
+def test_pruning_is_exact(mvs, best_k, refine, interp):
+    import synthetic as S
+
+    cap = S.tabletop(width=240, height=180, f=1450.0 * 240 / 1920, num_sources=8, seed=41)
+    sph = scene(128, 96, 4, 42)
+    items = [(views_of(mvs, S.as_reference(cap, 0)), cfg(mvs, cap, iterations=4)),
+             (views_of(mvs, sph), cfg(mvs, sph, iterations=4))]
+    common = dict(mode=mvs.MODE_PLANE, best_k=best_k, device=0, refine=refine, interp=interp,
+                  storage=mvs.STORAGE_FP16 if interp else mvs.STORAGE_FP32)
+    out, stats = [], []
+    for exhaustive in (0, 1):
+        eng = mvs.Engine(mvs.Options(exhaustive=exhaustive, **common))
+        try:
+            jobs = [eng.stage(v, c, undistort=True) for v, c in items]
+            eng.run_many(jobs)
+            out.append([eng.download(j) for j in jobs])
+            stats.append(eng.stats())
+        finally:
+            eng.close()
+    same(out[0], out[1])
+    pruned, full = stats[0], stats[1]
+    print(f"best_k={best_k}: hypotheses {pruned.hypotheses_evaluated} / {full.hypotheses_evaluated}, windows "
+          f"{pruned.windows_evaluated} / {full.windows_evaluated}")
+    assert pruned.hypotheses_evaluated == full.hypotheses_evaluated
+    assert pruned.windows_evaluated < full.windows_evaluated
