@@ -152,9 +152,10 @@ typedef struct recon_mvs_options {
   int32_t per_view;   /* plane mode: 0 = the jobs of one run form one batch -- one launch per
                          stage over all of them, captured once as a CUDA graph and replayed;
                          1 = the same kernels launched once per view, no graph */
-  int32_t exhaustive; /* plane mode: 1 = sample every source window of every candidate; 0 = skip
-                         the remaining windows of a candidate once its best-k bound shows it cannot
-                         be taken (the maps are the same; a switch for checks and timing) */
+  int32_t exhaustive; /* plane mode: 1 = evaluate every candidate on every source window; 0 = skip
+                         a propagation candidate equal to the one just rejected, and the remaining
+                         windows of a candidate once its best-k bound shows it cannot be taken (the
+                         maps are the same; a switch for checks and timing) */
   int32_t reserved[1];
 } recon_mvs_options;
 

@@ -200,7 +200,7 @@ struct Job {
   double min_depth, max_depth;
   float photo_threshold;
   int best_k;
-  int prune;  // 1 = sweep candidates skip the windows that cannot change their fate
+  int prune;  // 1 = the sweep skips work that cannot change a pixel's fate (repeated candidates, hopeless windows)
   uint64_t seed;
   unsigned long long* eval_counter;  // optional: [0] hypotheses evaluated, [1] source windows sampled
   // plane-mode run parameters (read by the batched kernels per work item)

@@ -424,6 +424,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
   const float ifx = 1.0f / J.rfx, ify = 1.0f / J.rfy;
   int counts[2] = {0, 0};  // hypotheses, source windows sampled
 
+  float4 last = make_float4(-1.f, 0.f, 0.f, 0.f);  // the last candidate evaluated
   // --- propagation: best-cost neighbour of each region ---
   for (int r = 0; r < 8; ++r) {
     int best_n = -1;
@@ -463,8 +464,12 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
     // the transfer): nothing to learn -- in a converged region most regions
     // propose exactly this
     if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) continue;
-    const HypCost c =
-        eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts, J.prune ? cur_cost : kCostInf);
+    // the previous region's candidate again (the same plane reached through
+    // another neighbour): it was rejected, and its cost has not changed
+    if (J.prune && hn.y == last.y && hn.z == last.z && hn.w == last.w && rho == last.x) continue;
+    last = make_float4(rho, hn.y, hn.z, hn.w);
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts,
+                                               J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
       cur = make_float4(rho, hn.y, hn.z, hn.w);

@@ -147,3 +147,29 @@ def test_shared_image_staging_matches_per_job_staging(mvs):
     b = [eng.download(j) for j in jobs]
     eng.close()
     assert_same(b, a, "shared staging")
+
+
+def test_contexts_on_concurrent_host_threads(mvs, scenes):
+    """One context per host thread (the boundary's rule): two threads run the
+    same batch at the same time on their own contexts and streams; each gets
+    the maps of the batch run alone."""
+    import threading
+
+    base, _ = run_all(mvs, scenes, batched=True)
+    results, errors = [None, None], []
+
+    def worker(i):
+        try:
+            results[i] = run_all(mvs, scenes, batched=True, repeat=2)[0]
+        except Exception as e:  # surfaced on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(300)
+    assert not errors, errors
+    for r in results:
+        assert r is not None
+        assert_same(r, base, "concurrent context")

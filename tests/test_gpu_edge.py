@@ -5,8 +5,9 @@ bit-identical maps: images smaller than a tile or a window, a degenerate job
 (zero baseline) inside a batch, a job with zero iterations, mixed window
 sizes (two groups in one plan), 32 sources (the maximum; per-thread ray cache
 above 48 KB of shared memory), Gauss-Newton refinement on BF16 storage.
-The sweep's exact view pruning is checked the same way: with and without it
-the maps are bit-identical while fewer source windows are sampled.
+The sweep's exact shortcuts (repeated candidates skipped, hopeless windows
+pruned) are checked the same way: with and without them the maps are
+bit-identical while fewer source windows are sampled.
 """
 import numpy as np
 import pytest
@@ -138,5 +139,5 @@ def test_pruning_is_exact(mvs, best_k, refine, interp):
     pruned, full = stats[0], stats[1]
     print(f"best_k={best_k}: hypotheses {pruned.hypotheses_evaluated} / {full.hypotheses_evaluated}, windows "
           f"{pruned.windows_evaluated} / {full.windows_evaluated}")
-    assert pruned.hypotheses_evaluated == full.hypotheses_evaluated
+    assert pruned.hypotheses_evaluated <= full.hypotheses_evaluated
     assert pruned.windows_evaluated < full.windows_evaluated
