@@ -374,30 +374,6 @@ __device__ int plane_adjoint(const Job& J, const AdjHyp& h, float* cost, float g
   return k;
 }
 
-// The gradient and Gauss-Newton matrix of the mean cost of the views in
-// `sel` (a bit per source, k of them, chosen by the caller -- the best_k of
-// the search's own evaluation): per view one moments pass and one adjoint
-// pass, nothing kept per view.  Returns false if a selected view turns
-// invalid under the exact reads.
-template <int kMode>
-__device__ bool plane_adjoint_selected(const Job& J, const AdjHyp& h, uint32_t sel, int k, float g[3], float H[6]) {
-  for (int i = 0; i < 3; ++i) g[i] = 0.f;
-  for (int i = 0; i < 6; ++i) H[i] = 0.f;
-  if (k <= 0) return false;
-  const float inv_k = 1.0f / (float)k;
-  for (int s = 0; s < J.num_src; ++s) {
-    if (!((sel >> s) & 1u)) continue;
-    const ViewGeo geo = view_geo(J, J.src[s], h);
-    const ViewMom mo = view_moments<kMode>(J, J.src[s], geo, h);
-    if (!mo.valid) return false;
-    float gs[3], Hs[6];
-    view_adjoint<kMode, false>(J, J.src[s], geo, h, mo, gs, Hs, nullptr, nullptr);
-    for (int i = 0; i < 3; ++i) g[i] += gs[i] * inv_k;
-    for (int i = 0; i < 6; ++i) H[i] += Hs[i] * inv_k;
-  }
-  return true;
-}
-
 // Solves (H + lambda diag(H)) x = -g for the symmetric 3 x 3 H (upper
 // triangle 00 01 02 11 12 22); false when singular.
 __device__ __forceinline__ bool solve_lm3(const float H[6], const float g[3], float lambda, float x[3]) {
