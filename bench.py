@@ -835,7 +835,8 @@ def run_differentiable(args, n_hyp=10_000):
 
 def run_precision(args):
     """1 + 16 sources at 1920x1440 (40-160 mm baselines) on the tabletop
-    scene: each storage form timed (depth maps/s, one map per step), its
+    scene: each storage form (FP32, FP16, BF16, 8-bit; exact or texture-unit
+    interpolation) timed (depth maps/s, one map per step), its
     error vs analytic truth, and -- on a 160x120 centre crop run by both --
     its depth / normal difference to the FP64 oracle run of the same search."""
     import numpy as np
@@ -855,7 +856,9 @@ def run_precision(args):
     cfg = config_of(M, sc)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda:0")
     forms = {"fp32": (M.STORAGE_FP32, 0), "fp16": (M.STORAGE_FP16, 0), "bf16": (M.STORAGE_BF16, 0),
-             "fp16_texture_interp": (M.STORAGE_FP16, 1)}
+             "fp16_texture_interp": (M.STORAGE_FP16, 1),
+             # the bandwidth floor: 8-bit textures (the undistorted intensities rounded to 8 bits)
+             "u8": (M.STORAGE_U8, 0), "u8_texture_interp": (M.STORAGE_U8, 1)}
     # the crop: same cameras with the principal point shifted
     cw, ch = 160, 120
     x0, y0 = W // 2 - cw // 2, H // 2 - ch // 2

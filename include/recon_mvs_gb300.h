@@ -125,8 +125,11 @@ typedef enum recon_mvs_mode {
 typedef enum recon_mvs_storage {
   RECON_MVS_STORAGE_FP32 = 0, /* source images as FP32 textures */
   RECON_MVS_STORAGE_FP16 = 1, /* FP16 textures: exact for 8-bit input */
-  RECON_MVS_STORAGE_BF16 = 2  /* BF16 values (8-bit mantissa; an ablation of FP16) in 16-bit textures,
+  RECON_MVS_STORAGE_BF16 = 2, /* BF16 values (8-bit mantissa; an ablation of FP16) in 16-bit textures,
                                  read by 2x2 gather and widened exactly; plane mode, interp = 0 only */
+  RECON_MVS_STORAGE_U8 = 3    /* 8-bit textures read as I / 255 (NCC does not see the scale): the
+                                 bandwidth floor, exact for 8-bit input; resampled (undistorted)
+                                 intensities are rounded to 8 bits; plane mode only */
 } recon_mvs_storage;
 
 typedef struct recon_mvs_options {

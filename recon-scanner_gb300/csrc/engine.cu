@@ -322,8 +322,10 @@ struct Context {
     if (o.refine < 0 || o.refine > 2) fail(RECON_ERR_INVALID_ARGUMENT, "refine must be 0, 1 or 2");
     if (o.tile_rows != 0 && row_choice_index(o.tile_rows) < 0)
       fail(RECON_ERR_INVALID_ARGUMENT, "tile_rows must be 0 (autotuned), 2, 4 or 8");
-    if (o.storage < RECON_MVS_STORAGE_FP32 || o.storage > RECON_MVS_STORAGE_BF16)
+    if (o.storage < RECON_MVS_STORAGE_FP32 || o.storage > RECON_MVS_STORAGE_U8)
       fail(RECON_ERR_INVALID_ARGUMENT, "unknown storage format");
+    if (o.storage == RECON_MVS_STORAGE_U8 && o.mode != RECON_MVS_MODE_PLANE)
+      fail(RECON_ERR_INVALID_ARGUMENT, "U8 storage needs plane mode");
     if (o.storage == RECON_MVS_STORAGE_BF16 && (o.mode != RECON_MVS_MODE_PLANE || o.interp != 0))
       fail(RECON_ERR_INVALID_ARGUMENT, "BF16 storage needs plane mode with exact interpolation (interp = 0)");
     device = o.device;
@@ -393,16 +395,19 @@ static const recon_camera_intrinsics& src_intr(const recon_mvs_views& v, int k) 
 }
 
 // Source texture of (I - 128) in the context's storage format: FP32, FP16
-// (both with a point-filtered gather object and a linear-filter object) or
-// BF16 bits in a 16-bit unsigned channel (gather object only).
+// (both with a point-filtered gather object and a linear-filter object),
+// BF16 bits in a 16-bit unsigned channel (gather object only), or 8-bit
+// unsigned read as normalised floats, I / 255 (both objects).
 static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32, int w, int h, int storage,
                          Texture& T) {
   const bool bf16 = storage == RECON_MVS_STORAGE_BF16;
+  const bool u8 = storage == RECON_MVS_STORAGE_U8;
   cudaChannelFormatDesc desc = storage == RECON_MVS_STORAGE_FP16 ? cudaCreateChannelDescHalf()
                                : bf16 ? cudaCreateChannelDesc(16, 0, 0, 0, cudaChannelFormatKindUnsigned)
+                               : u8   ? cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned)
                                       : cudaCreateChannelDesc<float>();
   CK(cudaMallocArray(&T.arr, &desc, w, h, cudaArrayTextureGather));
-  const size_t elem = storage == RECON_MVS_STORAGE_FP32 ? 4 : 2;
+  const size_t elem = storage == RECON_MVS_STORAGE_FP32 ? 4 : u8 ? 1 : 2;
   const size_t pitch = ((size_t)w * elem + 255) & ~(size_t)255;
   C.stage_tex.alloc(pitch * h);
   if (is_f32)
@@ -420,7 +425,7 @@ static void make_texture(Context& C, const void* dev_img_u8_or_f32, bool is_f32,
   td.addressMode[0] = cudaAddressModeClamp;
   td.addressMode[1] = cudaAddressModeClamp;
   td.filterMode = cudaFilterModePoint;
-  td.readMode = cudaReadModeElementType;
+  td.readMode = u8 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
   td.normalizedCoords = 0;
   CK(cudaCreateTextureObject(&T.tex, &rd, &td, nullptr));
   if (!bf16) {

@@ -1094,11 +1094,15 @@ __global__ void k_deinterleave(const float* __restrict__ ref, int w, int h, int 
 
 // One staged source texel of (I - 128) in the storage format (0 FP32, 1 FP16,
 // 2 BF16 bits), rounded to nearest even.
+// One source texel, v = I - 128, in the storage format (0 FP32, 1 FP16,
+// 2 BF16 bits, 3 the 8-bit intensity I rounded to nearest and clamped).
 __device__ __forceinline__ void store_texel(void* out, size_t i, float v, int storage) {
   if (storage == 1)
     ((__half*)out)[i] = __float2half_rn(v);
   else if (storage == 2)
     ((unsigned short*)out)[i] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  else if (storage == 3)
+    ((uint8_t*)out)[i] = (uint8_t)__float2int_rn(fminf(255.0f, fmaxf(0.0f, v + 128.0f)));
   else
     ((float*)out)[i] = v;
 }
@@ -1349,10 +1353,12 @@ cudaError_t launch_prep_ref(const uint8_t* img, int w, int h, float* ref, float*
   return cudaGetLastError();
 }
 
+static size_t texel_bytes(int storage) { return storage == 0 ? 4 : storage == 3 ? 1 : 2; }
+
 cudaError_t launch_prep_src(const uint8_t* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                             cudaStream_t st) {
   const dim3 b(32, 8);
-  k_prep_src<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (storage == 0 ? 4 : 2), storage);
+  k_prep_src<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / texel_bytes(storage), storage);
   return cudaGetLastError();
 }
 
@@ -1365,7 +1371,7 @@ cudaError_t launch_prep_ref_f32(const float* img, int w, int h, float* ref, floa
 cudaError_t launch_prep_src_f32in(const float* img, int w, int h, void* out, size_t pitch_bytes, int storage,
                                   cudaStream_t st) {
   const dim3 b(32, 8);
-  k_prep_src_f32in<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / (storage == 0 ? 4 : 2), storage);
+  k_prep_src_f32in<<<grid2d(w, h, b), b, 0, st>>>(img, w, h, out, pitch_bytes / texel_bytes(storage), storage);
   return cudaGetLastError();
 }
 

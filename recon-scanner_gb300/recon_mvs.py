@@ -31,6 +31,7 @@ MODE_PLANE = 1
 STORAGE_FP32 = 0
 STORAGE_FP16 = 1
 STORAGE_BF16 = 2
+STORAGE_U8 = 3
 
 
 class Intrinsics(C.Structure):

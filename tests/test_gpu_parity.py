@@ -95,7 +95,8 @@ def plane_hypotheses(sc, n, seed):
 
 def test_plane_cost_matches_fp64_oracle(mvs, orc):
     """Plane-induced homography cost vs the FP64 oracle restatement on
-    identical hypotheses (FP16 and FP32 storage give identical 8-bit texels)."""
+    identical hypotheses (FP32, FP16 and 8-bit storage all hold the 8-bit
+    texels exactly; the 8-bit texture reads I / 255, a scale NCC ignores)."""
     import synthetic as S
 
     sc = S.sphere_on_backdrop(width=160, height=120, f=150.0, num_sources=4, seed=3)
@@ -107,7 +108,7 @@ def test_plane_cost_matches_fp64_oracle(mvs, orc):
     for best_k, sampling in ((0, 0), (2, 0), (2, 1)):
         want, want_sup, want_view = orc.plane_costs(vs_o, O.make_config(**cfg_d), best_k, px, py, inv, nrm,
                                                     half_pixel=sampling)
-        for storage in (mvs.STORAGE_FP32, mvs.STORAGE_FP16):
+        for storage in (mvs.STORAGE_FP32, mvs.STORAGE_FP16, mvs.STORAGE_U8):
             opts = mvs.Options(mode=mvs.MODE_PLANE, best_k=best_k, storage=storage, sampling=sampling)
             va = mvs.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
             got, sup, view = mvs.Evaluate(va, mvs.MvsConfig(**cfg_d), opts, px, py, inv, nrm.astype(np.float32),
