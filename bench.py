@@ -571,6 +571,18 @@ def run_gpu(args):
         traffic = prof.get("plane_sweep_bytes_per_launch", {}).get(key)
         tex_pipe = prof.get("plane_sweep_tex_data_pipe_pct", {}).get(key)
 
+    # the HBM side of the roofline, per half-sweep: the algorithmic bytes
+    # (every map's source images + its per-pixel state read and written:
+    # float4 plane + float cost + uint8 support = 21 B) over the sweep time,
+    # against the measured copy bandwidth
+    b_img = 2 if args.fp16 else 4
+    alg_bytes = sum((1 + ns) * px * b_img + 2 * px * 21 for px, ns in zip(pixels, n_src))
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_gbs = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    hbm_side = {"algorithmic_bytes_per_launch": alg_bytes, "achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak,
+                "frac": hbm_gbs / hbm_peak, "measured_dram_bytes_per_launch": traffic,
+                "peak_source": f"{peak_src} MEASURED_PEAKS.json hbm_gbs"}
+
     form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
             f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
             f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}")
@@ -605,6 +617,7 @@ def run_gpu(args):
                          "ms_per_launch": per_launch_ms, "flop_per_launch": flop_per_launch,
                          "flop_model": f"{flop_per_window} per source window sampled + {flop_per_hyp_setup} per "
                                        f"hypothesis",
+                         "hbm": hbm_side,
                          "binding_unit": {"unit": "L1TEX texture data pipe (bilinear source reads)",
                                           "pct_of_peak": tex_pipe,
                                           "source": "ncu l1tex__data_pipe_tex_wavefronts.avg."
