@@ -51,10 +51,11 @@ __device__ __forceinline__ void sph_normal(float t, float p, float n[3], float n
 // The hypothesis of one pixel in reference-camera terms.
 struct AdjHyp {
   int x, y;
-  float d;
+  float d, id;  // depth and 1 / depth
   float n[3], nt[3], np[3];
   float qc[3];  // pixel-centre ray
   float kappa;  // n . qc
+  float irfx, irfy;  // 1 / reference focal lengths: ray offsets dx / fx, dy / fy
 };
 
 // Per-view moments of the first pass (values shifted by the window-centre
@@ -125,7 +126,7 @@ __device__ __forceinline__ bool adj_sample(const Job& J, const SrcView& S, const
                                            float* mk, float q[2]) {
   const int rx = h.x + dx, ry = h.y + dy;
   if (rx < 0 || ry < 0 || rx > J.w - 1 || ry > J.h - 1) return false;
-  const float dq0 = (float)dx / J.rfx, dq1 = (float)dy / J.rfy;
+  const float dq0 = (float)dx * h.irfx, dq1 = (float)dy * h.irfy;
   const float ndq = h.n[0] * dq0 + h.n[1] * dq1;
   const float m = h.kappa + ndq;
   if (!(m < 0.0f)) return false;
@@ -252,8 +253,9 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
       for (int j = 0; j < 3; ++j) w[j] = A[j] * G[0] + A[3 + j] * G[1] + A[6 + j] * G[2];
       const float qx = q[0], qy = q[1];  // the sample's ray (z = 1)
       const float wq = w[0] * qx + w[1] * qy + w[2];
-      const float dd = (w[0] * X[0] + w[1] * X[1] + w[2] * X[2]) / h.d;
-      const float cn = wq * h.d / (m * m);
+      const float dd = (w[0] * X[0] + w[1] * X[1] + w[2] * X[2]) * h.id;
+      const float im = rcp_approx(m);
+      const float cn = wq * h.d * (im * im);
       float dn[3];
       dn[0] = cn * (h.qc[0] * m - h.kappa * qx);
       dn[1] = cn * (h.qc[1] * m - h.kappa * qy);
@@ -312,6 +314,9 @@ __device__ __forceinline__ bool make_adj_hyp(const Job& J, int x, int y, float d
   h->x = x;
   h->y = y;
   h->d = d;
+  h->id = 1.0f / d;
+  h->irfx = 1.0f / J.rfx;
+  h->irfy = 1.0f / J.rfy;
   sph_normal(theta, phi, h->n, h->nt, h->np);
   h->qc[0] = ((float)x + 0.5f - J.rcx) / J.rfx;
   h->qc[1] = ((float)y + 0.5f - J.rcy) / J.rfy;
