@@ -461,9 +461,25 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
 
 // H > 0: windows of 2H+1 known at compile time, reference samples through
 // `ref` on the fast path; H == 0: any window size (runtime loop).
+// The window's moments as the adjoint wants them (`mom`, optional): n, the
+// means of the reference and source values, and the centred sums of squares
+// and products -- from sums shifted by (rmean, sc): mean = shift + S / n,
+// centred = S2 - S S' / n.
+__device__ __forceinline__ void window_moments(float* mom, float n, float rmean, float sc, float sr, float srr,
+                                               float ss, float sss, float srs) {
+  const float inv_n = 1.0f / n;
+  mom[0] = n;
+  mom[1] = rmean + sr * inv_n;
+  mom[2] = sc + ss * inv_n;
+  mom[3] = srr - sr * sr * inv_n;
+  mom[4] = sss - ss * ss * inv_n;
+  mom[5] = srs - sr * ss * inv_n;
+}
+
 template <int H, int kMode, class Ref>
 __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
-                                                      const PlaneHyp& hp, const RefWindow& rw, const Ref& ref) {
+                                                      const PlaneHyp& hp, const RefWindow& rw, const Ref& ref,
+                                                      float* mom = nullptr) {
   ViewResult bad{0.0f, -1};  // nothing sampled
   ff u0, v0;
   float xz, mx, my;
@@ -527,18 +543,22 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   if constexpr (H > 0) {
     if (full) {
       plane_window_fast<H, kMode>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
+      if (mom) window_moments(mom, (float)(K * K), rw.mean, sc, 0.0f, rw.sxx, acc[2], acc[3], acc[4]);
       return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
     }
     if (rw.full && front) {
       // straddles a source border: masked samples, reference from the tile
       plane_window_masked<H, kMode>(S, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc, &n);
+      if (mom && n > 0.f) window_moments(mom, n, rw.mean, sc, acc[0], acc[1], acc[2], acc[3], acc[4]);
       return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
     }
   } else if (full) {
     plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+    if (mom) window_moments(mom, (float)(K * K), rw.mean, sc, 0.0f, rw.sxx, acc[2], acc[3], acc[4]);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
   plane_window<false, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  if (mom && n > 0.f) window_moments(mom, n, rw.mean, sc, acc[0], acc[1], acc[2], acc[3], acc[4]);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
 }
 

@@ -369,13 +369,32 @@ static void fill_defaults(recon_mvs_options* o) {
   o->device = 0;
 }
 
+// Largest image side: the texture-gather limit of the device, which also
+// keeps every pixel index (x + y * w) inside a 32-bit int.
+constexpr int kMaxImageSide = 32768;
+
+static void check_image_size(int w, int h, const char* what) {
+  if (w <= 0 || h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, std::string(what) + ": empty image");
+  if (w > kMaxImageSide || h > kMaxImageSide)
+    fail(RECON_ERR_INVALID_ARGUMENT, std::string(what) + ": image larger than 32768 pixels on a side");
+}
+
+// Pixels of a caller's depth map: 0 for a map without data or with a
+// non-positive size (an empty map contributes nothing, as in the reference's
+// loops); larger than the image limit is an error.
+static size_t map_pixels(const recon_mvs_depth_map& m) {
+  if (!m.depth || m.width <= 0 || m.height <= 0) return 0;
+  check_image_size(m.width, m.height, "depth map");
+  return (size_t)m.width * m.height;
+}
+
 // Contract checks of PatchMatchStereo (patchmatch_stereo.cpp:434-468).
 static bool intrinsics_global(const recon_mvs_views& v) { return v.num_src_intrinsics == v.num_src_poses; }
 
 static void validate_views(const recon_mvs_views* v) {
   if (!v) fail(RECON_ERR_INVALID_ARGUMENT, "views is NULL");
   if (!v->ref_gray || !v->ref_pose || !v->ref_intr) fail(RECON_ERR_INVALID_ARGUMENT, "reference image/pose/intrinsics NULL");
-  if (v->ref_w <= 0 || v->ref_h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "empty reference image");
+  check_image_size(v->ref_w, v->ref_h, "reference");
   if (v->num_src <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "no source views");
   if (v->num_src > kMaxSources) fail(RECON_ERR_INVALID_ARGUMENT, "more than 32 source views");
   if (!v->src_gray || !v->src_w || !v->src_h || !v->src_poses || !v->src_intrinsics || !v->source_indices)
@@ -386,7 +405,8 @@ static void validate_views(const recon_mvs_views* v) {
   for (int k = 0; k < v->num_src; ++k) {
     const int si = v->source_indices[k];
     if (si < 0 || si >= v->num_src_poses) fail(RECON_ERR_INVALID_ARGUMENT, "source index outside src_poses");
-    if (!v->src_gray[k] || v->src_w[k] <= 0 || v->src_h[k] <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "empty source image");
+    if (!v->src_gray[k]) fail(RECON_ERR_INVALID_ARGUMENT, "source image NULL");
+    check_image_size(v->src_w[k], v->src_h[k], "source");
   }
 }
 
@@ -514,7 +534,8 @@ static void zero_distortion(recon_camera_intrinsics* k) { k->k1 = k->k2 = k->k3 
 
 static std::shared_ptr<StagedImage> stage_image(Context& C, const uint8_t* host, int w, int h,
                                                 const recon_camera_intrinsics& k, bool undistort) {
-  if (!host || w <= 0 || h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "image NULL or empty");
+  if (!host) fail(RECON_ERR_INVALID_ARGUMENT, "image NULL");
+  check_image_size(w, h, "staged");
   auto I = std::make_shared<StagedImage>();
   I->w = w;
   I->h = h;
@@ -529,7 +550,8 @@ static std::shared_ptr<StagedImage> stage_image(Context& C, const uint8_t* host,
 // stage_image does.
 static std::shared_ptr<StagedImage> stage_image_bgra(Context& C, const uint8_t* bgra, int w, int h, int stride,
                                                      const recon_camera_intrinsics& k, bool undistort) {
-  if (!bgra || w <= 0 || h <= 0 || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "BGRA image NULL, empty or short rows");
+  check_image_size(w, h, "BGRA");
+  if (!bgra || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "BGRA image NULL or short rows");
   auto I = std::make_shared<StagedImage>();
   I->w = w;
   I->h = h;
@@ -1507,7 +1529,9 @@ RECON_API recon_status recon_mvs_compute_ncc(const uint8_t* ref, int32_t ref_w, 
                                              int32_t patch_size, recon_mvs_ncc_result* out) {
   return guard([&] {
     if (!ref || !src || (!coords && n > 0) || (!out && n > 0)) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (ref_w <= 0 || ref_h <= 0 || src_w <= 0 || src_h <= 0 || n < 0) fail(RECON_ERR_INVALID_ARGUMENT, "bad size");
+    check_image_size(ref_w, ref_h, "reference");
+    check_image_size(src_w, src_h, "source");
+    if (n < 0) fail(RECON_ERR_INVALID_ARGUMENT, "negative window count");
     if (n == 0) return;
     Context& C = default_context(nullptr);
     C.use();
@@ -1921,16 +1945,16 @@ RECON_API recon_status recon_mvs_geometric_consistency(const recon_mvs_depth_map
     std::vector<std::unique_ptr<DevArray<float>>> dev(num_maps);
     for (int m = 0; m < num_maps; ++m) {
       dev[m] = std::make_unique<DevArray<float>>();
-      if (!maps[m].depth) continue;
-      const size_t n = (size_t)maps[m].width * maps[m].height;
+      const size_t n = map_pixels(maps[m]);
+      if (n == 0) continue;
       dev[m]->alloc(n);
       CK(cudaMemcpyAsync(dev[m]->p, maps[m].depth, n * sizeof(float), cudaMemcpyHostToDevice, C.stream));
     }
     const recon_mvs_depth_map& R = maps[ref_index];
-    if (!R.depth) fail(RECON_ERR_INVALID_ARGUMENT, "reference map NULL");
+    if (map_pixels(R) == 0) fail(RECON_ERR_INVALID_ARGUMENT, "reference map NULL or empty");
     std::vector<DevMap> others;
     for (int s = 0; s < num_maps; ++s)
-      if (s != ref_index && maps[s].depth)
+      if (s != ref_index && dev[s]->p)
         others.push_back(DevMap{maps[s].width, maps[s].height, dev[s]->p, intr[s], poses[s]});
     const size_t n = (size_t)R.width * R.height;
     DevArray<uint8_t> dc, dk;
@@ -2102,9 +2126,9 @@ RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const rec
     std::vector<std::unique_ptr<DevArray<uint8_t>>> dsup, dkeep;
     std::vector<FuseMap> fm;
     for (int m = 0; m < num_maps; ++m) {
-      if (!maps[m].depth) continue;
+      const size_t n = map_pixels(maps[m]);
+      if (n == 0) continue;
       if (!maps[m].support_count || !maps[m].confidence) fail(RECON_ERR_INVALID_ARGUMENT, "map arrays NULL");
-      const size_t n = (size_t)maps[m].width * maps[m].height;
       dd.push_back(std::make_unique<DevArray<float>>());
       dc.push_back(std::make_unique<DevArray<float>>());
       dsup.push_back(std::make_unique<DevArray<uint8_t>>());
@@ -2131,7 +2155,8 @@ RECON_API recon_status recon_mvs_fuse(const recon_mvs_depth_map* maps, const rec
 RECON_API recon_status recon_mvs_undistort(const uint8_t* img, int32_t w, int32_t h,
                                            const recon_camera_intrinsics* intr, float* out) {
   return guard([&] {
-    if (!img || !intr || !out || w <= 0 || h <= 0) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    if (!img || !intr || !out) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    check_image_size(w, h, "undistort");
     Context& C = default_context(nullptr);
     C.use();
     DevArray<uint8_t> di;
@@ -2203,7 +2228,8 @@ RECON_API recon_status recon_mvs_image_stage_bgra(void* ctx, const uint8_t* bgra
 RECON_API recon_status recon_mvs_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride,
                                               uint8_t* out) {
   return guard([&] {
-    if (!bgra || !out || w <= 0 || h <= 0 || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
+    check_image_size(w, h, "BGRA");
+    if (!bgra || !out || stride < 4 * w) fail(RECON_ERR_INVALID_ARGUMENT, "bad argument");
     Context& C = default_context(nullptr);
     C.use();
     DevArray<uint8_t> dev, g;

@@ -29,6 +29,8 @@ namespace rmvs {
 constexpr int kNoAllocMaxSources = 64;
 
 static __device__ __align__(256) ConsistencySrc g_noalloc_sources[kNoAllocMaxSources];
+// Largest map side: keeps every pixel index inside a 32-bit int.
+constexpr int kNoAllocMaxSide = 32768;
 
 // the per-thread error text that recon_mvs_last_error() returns (engine.cu)
 extern thread_local std::string g_last_error;
@@ -82,14 +84,19 @@ extern "C" RECON_API recon_status recon_mvs_geometric_consistency_noalloc(
     int32_t ref_index, float rel_depth_max, float reproj_px_max, int32_t min_views, uint8_t* out_count,
     uint8_t* out_keep, void* stream) {
   if (!maps || !poses || !intr || num_maps <= 0 || ref_index < 0 || ref_index >= num_maps || !out_count ||
-      !out_keep || !maps[ref_index].depth || maps[ref_index].width <= 0 || maps[ref_index].height <= 0) {
+      !out_keep || !maps[ref_index].depth || maps[ref_index].width <= 0 || maps[ref_index].height <= 0 ||
+      maps[ref_index].width > kNoAllocMaxSide || maps[ref_index].height > kNoAllocMaxSide) {
     g_last_error = "geometric_consistency_noalloc: NULL pointer or bad map/index";
     return RECON_ERR_INVALID_ARGUMENT;
   }
   ConsistencySrc table[kNoAllocMaxSources];
   int n = 0;
   for (int s = 0; s < num_maps; ++s) {
-    if (s == ref_index || !maps[s].depth) continue;
+    if (s == ref_index || !maps[s].depth || maps[s].width <= 0 || maps[s].height <= 0) continue;
+    if (maps[s].width > kNoAllocMaxSide || maps[s].height > kNoAllocMaxSide) {
+      g_last_error = "geometric_consistency_noalloc: a map larger than 32768 pixels on a side";
+      return RECON_ERR_INVALID_ARGUMENT;
+    }
     if (n == kNoAllocMaxSources) {
       g_last_error = "geometric_consistency_noalloc: more than 64 source maps (the fixed descriptor array's size)";
       return RECON_ERR_INVALID_ARGUMENT;

@@ -1001,6 +1001,64 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine(const __grid_constant__
 // steps on (d, theta, phi) from the adjoint of the aggregated cost (exact
 // bilinear reads, window recomputed per pass), each step accepted only when
 // the search's own cost of the new plane is lower.
+// The gradient and Gauss-Newton matrix of the aggregated cost for one
+// refinement step: each view's moments (and from them the best_k selection)
+// by the search's own window code with exact 2x2 reads -- an incremental
+// homography walk -- then the adjoint's Jacobian pass over the selected
+// views only.  False for an invalid hypothesis.
+template <int H, int kMode, class Ref>
+__device__ bool gn_gradient(const Job& J, const PCache& pc, int x, int y, float rx, float ry, const AdjHyp& h,
+                            const RefWindow& rw, const Ref& ref, float g[3], float Hm[6]) {
+  constexpr int kExact = kMode == kSrcBf16 ? kSrcBf16 : kSrcExact;
+  for (int i = 0; i < 3; ++i) g[i] = 0.f;
+  for (int i = 0; i < 6; ++i) Hm[i] = 0.f;
+  PlaneHyp hp;
+  if (!make_plane_hyp(J, rx, ry, 1.0f / h.d, h.n[0], h.n[1], h.n[2], &hp)) return false;
+  const int ns = min(J.num_src, kMaxSources);
+  ViewMom mom[kMaxSources];
+  float vc[kMaxSources];
+  int nvalid = 0;
+  for (int s = 0; s < ns; ++s) {
+    ff P[3];
+    pc.get(s, P);
+    float m[6];
+    const ViewResult v = eval_view_plane<H, kExact>(J, J.src[s], x, y, P, hp, rw, ref, m);
+    mom[s].valid = v.valid > 0;
+    vc[s] = kCostInf;
+    if (mom[s].valid) {
+      mom[s].n = m[0];
+      mom[s].mr = m[1];
+      mom[s].ms = m[2];
+      mom[s].srr = m[3];
+      mom[s].sss = m[4];
+      mom[s].srs = m[5];
+      mom[s].ncc = v.ncc;
+      vc[s] = 1.0f - v.ncc;
+      ++nvalid;
+    }
+  }
+  if (nvalid == 0) return false;
+  const int k = (J.best_k <= 0 || J.best_k >= nvalid || J.best_k > kMaxBestK) ? nvalid : J.best_k;
+  // the k lowest costs, ties to the lower source index
+  uint32_t sel = 0;
+  for (int t = 0; t < k; ++t) {
+    int b = -1;
+    for (int s = 0; s < ns; ++s)
+      if (mom[s].valid && !((sel >> s) & 1u) && (b < 0 || vc[s] < vc[b])) b = s;
+    sel |= 1u << b;
+  }
+  const float inv_k = 1.0f / (float)k;
+  for (int s = 0; s < ns; ++s) {
+    if (!((sel >> s) & 1u)) continue;
+    float gs[3], Hs[6];
+    const ViewGeo geo = view_geo(J, J.src[s], h);
+    view_adjoint<kMode, false>(J, J.src[s], geo, h, mom[s], gs, Hs, nullptr, nullptr);
+    for (int i = 0; i < 3; ++i) g[i] += gs[i] * inv_k;
+    for (int i = 0; i < 6; ++i) Hm[i] += Hs[i] * inv_k;
+  }
+  return true;
+}
+
 template <int H, int kMode>
 __global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constant__ PlaneBatch B) {
   extern __shared__ float2 smem[];
@@ -1026,8 +1084,8 @@ __global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constan
   for (int it = 0; it < J.refine_iters; ++it) {
     AdjHyp ah;
     if (!make_adj_hyp(J, x, y, d, theta, phi, &ah)) break;
-    float c, g[3], Hm[6];
-    if (plane_adjoint<kMode>(J, ah, &c, g, Hm, nullptr) == 0) break;
+    float g[3], Hm[6];
+    if (!gn_gradient<H, kMode>(J, pc, x, y, rx, ry, ah, rw, ref, g, Hm)) break;
     bool accepted = false;
     for (int t = 0; t < 4 && !accepted; ++t) {
       float step[3];

@@ -320,6 +320,18 @@ def test_contract_violations(mvs):
                         list(d["intr"])[:3], [1, 2, 3, 4])
     with pytest.raises(mvs.MvsError):
         mvs.PatchMatchStereo(bad2, cfg)
+    # images beyond the 32768-pixel side (the texture-gather limit, which
+    # also keeps pixel indices in 32 bits) are refused before any device work
+    wide = np.zeros((1, 40000), np.uint8)
+    bad3 = mvs.ViewArgs(wide, [wide], d["ref_pose"], [d["poses"][1]], d["ref_intr"], [d["intr"][1]], [0])
+    with pytest.raises(mvs.MvsError) as e:
+        mvs.PatchMatchStereo(bad3, cfg)
+    assert e.value.status == mvs.RECON_ERR_INVALID_ARGUMENT
+    eng = mvs.Engine(mvs.Options(mode=mvs.MODE_PLANE, device=0))
+    with pytest.raises(mvs.MvsError) as e:
+        eng.stage_image(wide, d["ref_intr"])
+    assert e.value.status == mvs.RECON_ERR_INVALID_ARGUMENT
+    eng.close()
     # empty depth range: RECON_OK, nothing filled (patchmatch_stereo.cpp:485)
     cfg2 = gpu_config(mvs, d)
     cfg2.min_depth_m, cfg2.max_depth_m = 0.9, 0.5
