@@ -6,6 +6,10 @@
 // colour reading only the other colour, so it is race-free and
 // deterministic -- with adaptive neighbour selection (best cost in each of 8
 // regions) and random perturbation; cost = mean of the best_k view costs.
+// Work that cannot change a pixel's fate is skipped (a propagation candidate
+// equal to the one just rejected; the remaining source windows of a
+// candidate once its best-k bound rules it out): the maps do not depend on
+// it, and Job::prune = 0 turns it off.
 //
 // Compat mode (drop-in parity): the reference PatchMatchStereo exactly --
 // fronto-parallel inverse-depth hypotheses, translated windows, and the
