@@ -1064,7 +1064,7 @@ __device__ bool gn_gradient(const Job& J, const PCache& pc, int x, int y, float 
 }
 
 template <int H, int kMode>
-__global__ void __launch_bounds__(128, 4) k_plane_refine_gn(const __grid_constant__ PlaneBatch B) {
+__global__ void __launch_bounds__(128, 5) k_plane_refine_gn(const __grid_constant__ PlaneBatch B) {
   extern __shared__ float2 smem[];
   const int tid = threadIdx.y * 32 + threadIdx.x;
   int j, x, y;
