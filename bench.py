@@ -255,11 +255,24 @@ def cpu_reference_sample(sc, cols=480, refine_rows=4, threads=None):
     return total, threads, note
 
 
+def describe_workload(scenes):
+    """The workload in words, shared by both arms of the bench."""
+    n_src = [len(sc.sources) for sc in scenes]
+    if WORKLOAD == "c2":
+        return (f"tabletop capture: 9 views {W}x{H} (k1=0.05, k2=-0.01, undistorted on the device), each the "
+                f"reference of one map with the other {S_SRC} as sources")
+    if WORKLOAD == "c3":
+        return (f"orbit capture: {len(scenes)} references from 120 frames, mixed 640x480/1280x960/1920x1440, "
+                f"{min(n_src)}-{max(n_src)} sources")
+    return f"sphere {W}x{H}, {S_SRC} sources"
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_init()
     if rank != 0:
         return
-    sc = make_scenes("cpu")[0]
+    scenes = make_scenes("cpu")
+    sc = scenes[0]
     secs = []
     threads = os.cpu_count() or 1
     note = ""
@@ -271,9 +284,11 @@ def run_reference_arm(args):
     value = 1.0 / per_map
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_map * 1000.0, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tabletop scene, analytic truth)",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scenes, analytic truth)",
             "impl": "reference",
-            "config": {"workload": f"tabletop {W}x{H}, {S_SRC} sources, {K}x{K}, {ITERS} iterations",
+            "config": {"workload": f"{describe_workload(scenes)}; {K}x{K}, {ITERS} iterations",
+                       "algorithm": "the reference's PatchMatchStereo + RefineSubpixel (FP64, host threads), "
+                                    "timed per depth map on map 0 of the workload",
                        "parallelism": "host threads"},
             "cpu_baseline": {"value": value, "unit": "depth maps/s", "cores": threads, "kind": "port",
                              "sample": note},
@@ -586,14 +601,7 @@ def run_gpu(args):
     form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
             f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
             f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}")
-    if WORKLOAD == "c2":
-        wl = (f"tabletop capture: 9 views {W}x{H} (k1=0.05, k2=-0.01, undistorted on the device), each the "
-              f"reference of one map with the other {S_SRC} as sources")
-    elif WORKLOAD == "c3":
-        wl = (f"orbit capture: {n_maps} references from 120 frames, mixed 640x480/1280x960/1920x1440, "
-              f"{min(n_src)}-{max(n_src)} sources")
-    else:
-        wl = f"sphere {W}x{H}, {S_SRC} sources"
+    wl = describe_workload(scenes)
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp16 storage)" if args.fp16 else "f32",
