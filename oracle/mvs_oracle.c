@@ -1098,9 +1098,16 @@ static int sample_source(const orc_views* v, int k, double u, double vv, int hal
   return sample_centre(v->src[k], v->src_w[k], v->src_h[k], u, vv, out);
 }
 
-orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32_t best_k,
-                                int32_t x, int32_t y, double inv_depth, const double n[3],
-                                int32_t half_pixel) {
+/* The plane cost with an optional bar: a caller that keeps the hypothesis
+ * only if its cost is below `beat` may stop once the views evaluated so far
+ * bound the final cost above it -- view costs lie in [0, 2], so with K views
+ * averaged (best_k, or all), n valid so far and r views left the final cost
+ * is at least (sum of the min(K, n + r) - r lowest costs so far) /
+ * min(K, n + r).  A stopped evaluation returns cost 1e30 (rejected, as the
+ * full one would be); beat >= 1e299 evaluates every view. */
+static orc_plane_result plane_cost_core(const orc_views* v, const orc_config* cfg, int32_t best_k,
+                                        int32_t x, int32_t y, double inv_depth, const double n[3],
+                                        int32_t half_pixel, double beat) {
   orc_plane_result res;
   memset(&res, 0, sizeof(res));
   res.cost = 1e30;
@@ -1123,7 +1130,32 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
   center_world(v->ref_pose, refc);
   int nvalid = 0;
   double vcost[32];
-  for (int k = 0; k < v->num_src && k < 32; ++k) {
+  const int nsrc = v->num_src < 32 ? v->num_src : 32;
+  for (int k = 0; k < nsrc; ++k) {
+    if (beat < 1e299 && nvalid > 0) {
+      const int left = nsrc - k;
+      const int K = best_k > 0 ? best_k : nsrc;
+      const int kk = K < nvalid + left ? K : nvalid + left;
+      const int j = kk - left;
+      if (j > 0) {
+        double low[32];
+        for (int i = 0; i < nvalid; ++i) { /* the costs so far, ascending */
+          int q = i;
+          while (q > 0 && low[q - 1] > vcost[i]) {
+            low[q] = low[q - 1];
+            --q;
+          }
+          low[q] = vcost[i];
+        }
+        double lb = 0.0;
+        for (int i = 0; i < j; ++i) lb += low[i];
+        if (lb > beat * (1.0 + 1e-12) * kk) {
+          res.cost = 1e30;
+          res.valid_views = 0;
+          return res;
+        }
+      }
+    }
     const orc_pose* sp = &v->src_poses[v->source_indices[k]];
     const orc_intrinsics* ks = src_intrinsics(v, k);
     /* A = R_s R_r^T, b = t_s - A t_r: reference-camera point -> source camera */
@@ -1211,6 +1243,12 @@ orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32
   res.cost = s / kk;
   if (res.cost > 3.0 * cfg->photo_threshold) res.cost = 1e30;
   return res;
+}
+
+orc_plane_result orc_plane_cost(const orc_views* v, const orc_config* cfg, int32_t best_k,
+                                int32_t x, int32_t y, double inv_depth, const double n[3],
+                                int32_t half_pixel) {
+  return plane_cost_core(v, cfg, best_k, x, y, inv_depth, n, half_pixel, 1e300);
 }
 
 typedef struct {
@@ -1454,13 +1492,17 @@ typedef struct {
   int32_t* support;
   int stage; /* 0 init, 1 sweep, 2 refine */
   int color, iter;
+  int prune; /* 1: the engine's exact shortcuts (stop a hopeless candidate, skip a repeated one) */
   int y0, y1;
 } pm_task;
 
-static double pm_eval(const pm_task* T, int x, int y, double rho, const double n[3], int32_t* support) {
+/* The cost of a hypothesis; a sweep candidate passes the pixel's cost as
+ * `beat` (kept only if below it), everything else 1e300. */
+static double pm_eval(const pm_task* T, int x, int y, double rho, const double n[3], int32_t* support,
+                      double beat) {
   *support = 0;
   if (!(rho > 0.0) || rho < T->rho_min || rho > T->rho_max) return 1e30;
-  const orc_plane_result r = orc_plane_cost(T->v, T->cfg, T->best_k, x, y, rho, n, 0);
+  const orc_plane_result r = plane_cost_core(T->v, T->cfg, T->best_k, x, y, rho, n, 0, T->prune ? beat : 1e300);
   *support = r.valid_views;
   return r.cost;
 }
@@ -1484,7 +1526,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
     double n[3];
     pm_random_normal(&g, rx, ry, n);
     int32_t sup;
-    T->cost[idx] = pm_eval(T, x, y, rho, n, &sup);
+    T->cost[idx] = pm_eval(T, x, y, rho, n, &sup, 1e300);
     T->support[idx] = sup;
     h[0] = rho;
     h[1] = n[0];
@@ -1496,6 +1538,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
     double cur[4] = {h[0], h[1], h[2], h[3]};
     double cur_cost = T->cost[idx];
     int32_t cur_sup = T->support[idx];
+    double last[4] = {-1.0, 0.0, 0.0, 0.0};
     for (int r = 0; r < 8; ++r) {
       int best_n = -1;
       double best_c = 1e30;
@@ -1528,9 +1571,15 @@ static void pm_pixel(const pm_task* T, int x, int y) {
       if (!(rho > 0.0)) continue;
       /* the current plane again: same normal, inverse depth within 4e-6 relative */
       if (hn[1] == cur[1] && hn[2] == cur[2] && hn[3] == cur[3] && fabs(rho - cur[0]) <= 4e-6 * cur[0]) continue;
+      /* the candidate just rejected again (its cost cannot have fallen) */
+      if (T->prune && hn[1] == last[1] && hn[2] == last[2] && hn[3] == last[3] && rho == last[0]) continue;
+      last[0] = rho;
+      last[1] = hn[1];
+      last[2] = hn[2];
+      last[3] = hn[3];
       const double n[3] = {hn[1], hn[2], hn[3]};
       int32_t sup;
-      const double c = pm_eval(T, x, y, rho, n, &sup);
+      const double c = pm_eval(T, x, y, rho, n, &sup, cur_cost);
       if (c < cur_cost) {
         cur_cost = c;
         cur[0] = rho;
@@ -1558,7 +1607,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
         if (q & 2) pm_perturb_normal(&g, rx, ry, 0.5 * scale, n);
       }
       int32_t sup;
-      const double c = pm_eval(T, x, y, rho, n, &sup);
+      const double c = pm_eval(T, x, y, rho, n, &sup, cur_cost);
       if (c < cur_cost) {
         cur_cost = c;
         cur[0] = rho;
@@ -1585,7 +1634,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
     const double inv_phi = 0.618033988749895;
     double c1 = hi - inv_phi * (hi - lo), c2 = lo + inv_phi * (hi - lo);
     int32_t s1, s2, sm;
-    double f1 = pm_eval(T, x, y, c1, n, &s1), f2 = pm_eval(T, x, y, c2, n, &s2);
+    double f1 = pm_eval(T, x, y, c1, n, &s1, 1e300), f2 = pm_eval(T, x, y, c2, n, &s2, 1e300);
     for (int q = 0; q < T->cfg->subpixel_iterations; ++q) {
       if (f1 < f2) {
         hi = c2;
@@ -1593,18 +1642,18 @@ static void pm_pixel(const pm_task* T, int x, int y) {
         f2 = f1;
         s2 = s1;
         c1 = hi - inv_phi * (hi - lo);
-        f1 = pm_eval(T, x, y, c1, n, &s1);
+        f1 = pm_eval(T, x, y, c1, n, &s1, 1e300);
       } else {
         lo = c1;
         c1 = c2;
         f1 = f2;
         s1 = s2;
         c2 = lo + inv_phi * (hi - lo);
-        f2 = pm_eval(T, x, y, c2, n, &s2);
+        f2 = pm_eval(T, x, y, c2, n, &s2, 1e300);
       }
     }
     const double mid = 0.5 * (lo + hi);
-    const double fm = pm_eval(T, x, y, mid, n, &sm);
+    const double fm = pm_eval(T, x, y, mid, n, &sm, 1e300);
     if (fm < best_c) {
       best_c = fm;
       best_d = mid;
@@ -1655,6 +1704,11 @@ static void pm_run_stage(const pm_task* base, int threads) {
 
 uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
                               int32_t refine, float* depth, float* normal, float* cost_out) {
+  return orc_plane_patchmatch_ex(v, cfg, best_k, seed, refine, 0, depth, normal, cost_out);
+}
+
+uint32_t orc_plane_patchmatch_ex(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                                 int32_t refine, int32_t prune, float* depth, float* normal, float* cost_out) {
   const size_t n = (size_t)v->ref_w * v->ref_h;
   for (size_t i = 0; i < n; ++i) {
     depth[i] = NAN;
@@ -1670,6 +1724,7 @@ uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t
   T.cfg = cfg;
   T.best_k = best_k;
   T.seed = seed;
+  T.prune = prune != 0;
   T.rho_min = inv_min;
   T.rho_max = inv_max;
   T.inv_per_px = 1.0 / (0.5 * (k->fx + k->fy) * baseline);

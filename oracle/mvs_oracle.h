@@ -223,6 +223,12 @@ void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, 
  * (optional) 3 floats per pixel; cost (optional).  Returns the filled count. */
 uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
                               int32_t refine, float* depth, float* normal, float* cost);
+/* The same with prune = 1: the engine's exact shortcuts (a sweep candidate
+ * stops once its views bound its cost above the pixel's; a propagation
+ * candidate equal to the one just rejected is skipped).  The maps are the
+ * ones prune = 0 gives. */
+uint32_t orc_plane_patchmatch_ex(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                                 int32_t refine, int32_t prune, float* depth, float* normal, float* cost);
 
 /* Geometric consistency (spec: shaders/vulkan/recon_mvs_consistency.comp:94-140
  * with the strict transform of shaders/common/gpu_algo.h:537-538, plus a

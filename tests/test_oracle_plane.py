@@ -5,7 +5,9 @@ restatement the device's plane mode is checked against).
     every view and the aggregate are infinite, as on the device;
   * NCC ignores an affine change of a source's intensities;
   * the analytic surface scores better than random planes at the same pixels;
-  * best_k = k is the mean of the k lowest view costs.
+  * best_k = k is the mean of the k lowest view costs;
+  * the engine's exact shortcuts, restated in the FP64 search, leave its maps
+    bit-identical.
 """
 import numpy as np
 import pytest
@@ -112,3 +114,18 @@ def test_best_k_is_the_mean_of_the_lowest_views(orc, scene):
             want = v[: min(k, len(v))].mean()
             assert cost[i] == pytest.approx(want, rel=1e-12, abs=1e-15)
             assert valid[i] == len(v)
+
+
+@pytest.mark.parametrize("best_k", [0, 2, 3])
+def test_exact_shortcuts_leave_the_fp64_search_unchanged(orc, scene, best_k):
+    """The engine's shortcuts restated in the FP64 search (a candidate stops
+    once its views bound its cost above the pixel's; a repeated propagation
+    candidate is skipped): the maps are bit-identical to the full search."""
+    sc = scene
+    c = O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=3, patch_size=11,
+                      subpixel_iterations=3, num_threads=4)
+    full = orc.plane_patchmatch(views(sc), c, best_k=best_k, refine=1, prune=False)
+    fast = orc.plane_patchmatch(views(sc), c, best_k=best_k, refine=1, prune=True)
+    assert full[0] == fast[0] > 0.5 * sc.ref.depth.size
+    for a, b in zip(full[1:], fast[1:]):
+        np.testing.assert_array_equal(a, b)
