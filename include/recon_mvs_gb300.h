@@ -435,17 +435,21 @@ RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out);
  * Same test as recon_mvs_geometric_consistency, but every map's `depth`
  * and out_count / out_keep (width*height of the reference map) are DEVICE
  * pointers owned by the caller; poses and intrinsics are host memory.  The
- * work is queued on `stream` (a cudaStream_t; NULL = the default stream) and
- * the call returns without waiting for it.  Nothing is allocated: the
+ * work is queued on `stream` (a cudaStream_t; NULL = the default stream).
+ * The descriptor table is uploaded from pageable host memory, so the call
+ * may block until the work already queued on that stream has drained; it
+ * does not wait for the consistency kernel itself.  Nothing is allocated: the
  * per-source descriptor table lives in a fixed array in the library's
  * device image, sized for at most 64 source maps (num_maps - 1 <= 64; more
  * is RECON_ERR_INVALID_ARGUMENT).  Every GPU that loads the library keeps
  * that array until the process exits.
  *
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's
- * contents; calls whose GPU work overlaps race on it, so serialise them. */
+ * Every call looks up the array's device address in the current CUDA
+ * context (the address belongs to the context, not to the device number);
+ * the first call in a context also loads the library's device image there,
+ * so make that first call before any stream capture.  All calls share the
+ * array and it keeps the last call's contents; calls whose GPU work overlaps
+ * race on it, so serialise them. */
 RECON_API recon_status recon_mvs_geometric_consistency_noalloc(const recon_mvs_depth_map* maps,
                                                                const recon_pose* poses,
                                                                const recon_camera_intrinsics* intr, int32_t num_maps,

@@ -151,20 +151,6 @@ static double mean_baseline(const recon_pose& ref, const recon_pose* poses, cons
 }
 
 // X_src = A X_ref + b with A = R_src R_ref^T, b = t_src - A t_ref
-static void relative_transform(const recon_pose& ref, const recon_pose& src, double A[9], double b[3]) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double s = 0.0;
-      for (int q = 0; q < 3; ++q) s += src.r[i * 3 + q] * ref.r[j * 3 + q];
-      A[i * 3 + j] = s;
-    }
-  for (int i = 0; i < 3; ++i) {
-    double s = 0.0;
-    for (int j = 0; j < 3; ++j) s += A[i * 3 + j] * ref.t[j];
-    b[i] = src.t[i] - s;
-  }
-}
-
 static ff ff_host(double d) {
   const float hi = (float)d;
   return ff{hi, (float)(d - (double)hi)};
@@ -821,8 +807,8 @@ static JobData& get_job(Context& C, int id) {
 // without a graph: the comparison the batched form is measured against.
 
 // The TMA view of a job's reference planes: a 3-D tensor {half_w, h, 2} of
-// FP32 with 16-byte row pitch, read in boxes of 48 columns x box_rows rows x
-// both planes (what one sweep tile stages), zeros outside.
+// FP32 with 16-byte row pitch, read in boxes of kTileCols columns x box_rows
+// rows x both planes (what one sweep tile stages), zeros outside.
 static void encode_ref_tile_map(const JobData& D, int box_rows, CUtensorMap* out) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
     void* fn = nullptr;
@@ -1902,27 +1888,7 @@ static void consistency_device(Context& C, const DevMap& ref, const std::vector<
                     (float)ref.intr.cy};
   std::vector<ConsistencySrc> srcs;
   for (const DevMap& o : others) {
-    ConsistencySrc cs;
-    std::memset(&cs, 0, sizeof(cs));
-    cs.w = o.w;
-    cs.h = o.h;
-    cs.depth = o.depth;
-    cs.fx = (float)o.intr.fx;
-    cs.fy = (float)o.intr.fy;
-    cs.cx = (float)o.intr.cx;
-    cs.cy = (float)o.intr.cy;
-    double A[9], b[3], Ai[9], bi[3];
-    relative_transform(ref.pose, o.pose, A, b);
-    relative_transform(o.pose, ref.pose, Ai, bi);
-    for (int i = 0; i < 9; ++i) {
-      cs.A[i] = (float)A[i];
-      cs.Ai[i] = (float)Ai[i];
-    }
-    for (int i = 0; i < 3; ++i) {
-      cs.b[i] = (float)b[i];
-      cs.bi[i] = (float)bi[i];
-    }
-    srcs.push_back(cs);
+    srcs.push_back(consistency_source(o.w, o.h, o.depth, o.intr, ref.pose, o.pose));
   }
   DevArray<ConsistencySrc> ds;
   ds.alloc(std::max<size_t>(1, srcs.size()));
@@ -2037,13 +2003,14 @@ static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_
   err.alloc(1);
   uint64_t cap = 1024;
   while (cap < 2 * (uint64_t)total) cap <<= 1;
+  // cap probed slots + the side slot of the one key equal to the empty marker
   tkey.alloc(cap);
-  tfirst.alloc(cap);
-  tcount.alloc(cap);
-  slot_vid.alloc(cap);
+  tfirst.alloc(cap + 1);
+  tcount.alloc(cap + 1);
+  slot_vid.alloc(cap + 1);
   CK(cudaMemsetAsync(tkey.p, 0x7F, cap * sizeof(unsigned long long), C.stream));
-  CK(cudaMemsetAsync(tfirst.p, 0xFF, cap * sizeof(unsigned long long), C.stream));
-  CK(cudaMemsetAsync(tcount.p, 0, cap * sizeof(unsigned int), C.stream));
+  CK(cudaMemsetAsync(tfirst.p, 0xFF, (cap + 1) * sizeof(unsigned long long), C.stream));
+  CK(cudaMemsetAsync(tcount.p, 0, (cap + 1) * sizeof(unsigned int), C.stream));
   CK(cudaMemsetAsync(err.p, 0, sizeof(int), C.stream));
   const FuseParams P{cfg.fusion_voxel_size_m, cfg.photo_threshold, cfg.min_view_consistency};
   for (size_t m = 0; m < maps.size(); ++m)

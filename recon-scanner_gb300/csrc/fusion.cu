@@ -17,7 +17,10 @@
 namespace rmvs {
 
 // Empty-slot key: the table is cleared with a byte memset of 0x7F, so the
-// sentinel must be that byte pattern.
+// sentinel must be that byte pattern.  A real voxel key can equal it (the
+// reference's key is a plain XOR of products): that one key never enters the
+// probed table and takes the reserved side slot `mask + 1` instead, so a
+// claimed slot is never mistaken for an empty one.
 constexpr unsigned long long kEmptyKey = 0x7F7F7F7F7F7F7F7Full;
 
 // ---------------------------------------------------------------------------
@@ -115,13 +118,22 @@ __device__ __forceinline__ unsigned long long hash64(unsigned long long x) {
   return x;
 }
 
-// Phase 2: hash insert; per slot count and first point index.
+// Phase 2: hash insert; per slot count and first point index.  table_key has
+// mask + 1 slots; table_count / table_first have one more, the side slot of
+// the key equal to kEmptyKey.
 __global__ void k_fuse_insert(int64_t n, const unsigned long long* __restrict__ key, const uint8_t* __restrict__ valid,
                               unsigned long long* table_key, unsigned int* table_count,
                               unsigned long long* table_first, uint64_t mask, int* slot_of, int* error) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n || !valid[g]) return;
   const unsigned long long k = key[g];
+  if (k == kEmptyKey) {
+    const uint64_t side = mask + 1;
+    atomicAdd(&table_count[side], 1u);
+    atomicMin(&table_first[side], (unsigned long long)g);
+    slot_of[g] = (int)side;
+    return;
+  }
   uint64_t s = hash64(k) & mask;
   for (uint64_t probe = 0; probe <= mask; ++probe) {
     const unsigned long long prev = atomicCAS(&table_key[s], kEmptyKey, k);

@@ -6,8 +6,10 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "common.cuh"
+#include "recon_mvs_gb300.h"
 
 namespace rmvs {
 
@@ -42,6 +44,51 @@ struct ConsistencySrc {
   float A[9], b[3];    // reference camera -> this camera
   float Ai[9], bi[3];  // this camera -> reference camera
 };
+
+// X_src = A X_ref + b with A = R_src R_ref^T and b = t_src - A t_ref, in FP64
+// and in this operation order: consistency counts and fused clouds are
+// compared bit for bit with the oracle, which composes the same way.  Every
+// caller (the allocating and the allocation-free consistency entry points,
+// the plane-mode job set-up) shares this one definition.
+inline void relative_transform(const recon_pose& ref, const recon_pose& src, double A[9], double b[3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) s += src.r[i * 3 + q] * ref.r[j * 3 + q];
+      A[i * 3 + j] = s;
+    }
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 3; ++j) s += A[i * 3 + j] * ref.t[j];
+    b[i] = src.t[i] - s;
+  }
+}
+
+// The consistency descriptor of one source map seen from the reference pose.
+inline ConsistencySrc consistency_source(int w, int h, const float* depth, const recon_camera_intrinsics& intr,
+                                         const recon_pose& ref_pose, const recon_pose& src_pose) {
+  ConsistencySrc cs;
+  memset(&cs, 0, sizeof(cs));
+  cs.w = w;
+  cs.h = h;
+  cs.depth = depth;
+  cs.fx = (float)intr.fx;
+  cs.fy = (float)intr.fy;
+  cs.cx = (float)intr.cx;
+  cs.cy = (float)intr.cy;
+  double A[9], b[3], Ai[9], bi[3];
+  relative_transform(ref_pose, src_pose, A, b);
+  relative_transform(src_pose, ref_pose, Ai, bi);
+  for (int i = 0; i < 9; ++i) {
+    cs.A[i] = (float)A[i];
+    cs.Ai[i] = (float)Ai[i];
+  }
+  for (int i = 0; i < 3; ++i) {
+    cs.b[i] = (float)b[i];
+    cs.bi[i] = (float)bi[i];
+  }
+  return cs;
+}
 
 struct UndistortCam {
   double fx, fy, cx, cy, k1, k2, k3, p1, p2;

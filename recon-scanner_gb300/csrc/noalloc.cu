@@ -18,7 +18,6 @@
 // writes every descriptor it reads, so nothing in it has to start at zero.
 // Calls whose work overlaps on the GPU (two streams, or two host threads)
 // race on the array; serialise them.
-#include <mutex>
 #include <string>
 
 #include "kernels.h"
@@ -37,41 +36,20 @@ extern thread_local std::string g_last_error;
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {};
-
-// Device address of the descriptor array on the current device, looked up
-// once per device.  In host code g_noalloc_sources is only a host-side
-// stand-in for the symbol, never a device address.
-cudaError_t scratch_address(int device, ConsistencySrc** out) {
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sources);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[device] = p;
-  }
-  *out = static_cast<ConsistencySrc*>(g_noalloc_ptr[device]);
+// Device address of the descriptor array in the CURRENT context.  In host
+// code g_noalloc_sources is only a host-side stand-in for the symbol, never a
+// device address.  The address belongs to a CUDA context, not to a device
+// number (a caller's own driver-API context, or a context re-created after
+// cudaDeviceReset, maps the array elsewhere), so it is looked up on every
+// call: the first call in a context loads the library's device image there
+// (the set-up; it allocates the array as part of that image), and later
+// calls are a table lookup that allocates nothing.
+cudaError_t scratch_address(ConsistencySrc** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sources);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<ConsistencySrc*>(p);
   return cudaSuccess;
-}
-
-// X_src = A X_ref + b with A = R_src R_ref^T, b = t_src - A t_ref, in the
-// operation order the consistency kernel's bit-exact contract assumes.
-void relative(const recon_pose& ref, const recon_pose& src, float Af[9], float bf[3]) {
-  double A[9];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double s = 0.0;
-      for (int q = 0; q < 3; ++q) s += src.r[i * 3 + q] * ref.r[j * 3 + q];
-      A[i * 3 + j] = s;
-    }
-  for (int i = 0; i < 3; ++i) {
-    double s = 0.0;
-    for (int j = 0; j < 3; ++j) s += A[i * 3 + j] * ref.t[j];
-    bf[i] = (float)(src.t[i] - s);
-  }
-  for (int i = 0; i < 9; ++i) Af[i] = (float)A[i];
 }
 
 }  // namespace
@@ -101,32 +79,18 @@ extern "C" RECON_API recon_status recon_mvs_geometric_consistency_noalloc(
       g_last_error = "geometric_consistency_noalloc: more than 64 source maps (the fixed descriptor array's size)";
       return RECON_ERR_INVALID_ARGUMENT;
     }
-    ConsistencySrc& c = table[n++];
-    c.w = maps[s].width;
-    c.h = maps[s].height;
-    c.depth = maps[s].depth;
-    c.fx = (float)intr[s].fx;
-    c.fy = (float)intr[s].fy;
-    c.cx = (float)intr[s].cx;
-    c.cy = (float)intr[s].cy;
-    relative(poses[ref_index], poses[s], c.A, c.b);
-    relative(poses[s], poses[ref_index], c.Ai, c.bi);
-  }
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess || device < 0 || device >= kMaxDevices) {
-    g_last_error = std::string("geometric_consistency_noalloc: no usable current device: ") + cudaGetErrorString(e);
-    return RECON_ERR_MVS_GPU_FAILURE;
+    table[n++] = consistency_source(maps[s].width, maps[s].height, maps[s].depth, intr[s], poses[ref_index], poses[s]);
   }
   ConsistencySrc* dev_table = nullptr;
-  e = scratch_address(device, &dev_table);
+  cudaError_t e = scratch_address(&dev_table);
   if (e != cudaSuccess) {
     g_last_error = std::string("geometric_consistency_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
     return RECON_ERR_MVS_GPU_FAILURE;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (n > 0) {
-    // pageable source: the call returns once `table` has been read
+    // pageable source: the runtime copies `table` out before returning, which
+    // may wait until the work already queued on the stream has drained
     e = cudaMemcpyAsync(dev_table, table, sizeof(ConsistencySrc) * n, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
       g_last_error = std::string("geometric_consistency_noalloc: table upload: ") + cudaGetErrorString(e);
