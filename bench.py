@@ -29,9 +29,12 @@ Other workloads: --workload small (C1, one 640x480 map), c3 (48 orbit
 references, batched vs per-view), c4 (the differentiation form), c5 (mixed
 precision).
 
-`--impl reference` times the reference algorithm on the host cores instead
-(the CPU oracle restatement of patchmatch_stereo.cpp, all threads) on a
-bounded sample of the same workload, extrapolated to one depth map.
+`--impl reference` times the reference's own CPU implementation on the host
+cores instead (its patchmatch_stereo.cpp compiled for this host, all
+threads; the oracle's restatement only where that cannot be built), one
+bounded tile sample of map 0 per step, extrapolated to whole depth maps;
+`--impl reference --full-map` times the whole map 0 once, beside every tile's
+estimate.
 
 Multi-GPU: the path does not shard (replicas only); each rank runs its own
 replica and value = total depth maps / max-over-ranks time.
@@ -190,69 +193,141 @@ def barrier(world):
 # CPU reference arm / baseline
 # ---------------------------------------------------------------------------
 
-def cpu_reference_sample(sc, cols=480, refine_rows=4, threads=None):
-    """Time the reference algorithm (the oracle's restatement of
-    patchmatch_stereo.cpp) on a crop of the workload and extrapolate to one
-    depth map.  The crop is 16 x threads rows tall -- the reference splits
-    its sweeps into min(threads, H/16) row blocks, so this keeps every
-    thread busy -- and `cols` wide, centred.  PatchMatch: initial cost + one
-    iteration (4 direction sweeps), scaled to ITERS iterations and the full
-    frame; RefineSubpixel (single-threaded in the reference) on
-    `refine_rows` rows, scaled to the frame.
-    Returns (seconds per depth map, threads, note)."""
-    import copy
-
-    import numpy as np
-
+def cpu_reference_impl():
+    """The CPU implementation that the reference arm and cpu_baseline time:
+    the reference's own patchmatch_stereo.cpp compiled for this host with
+    the reference's release flags (oracle/_ref/libref_mvs_release.so, from
+    the reference tree or its staged copy; kind "reference") where it can be built, else the oracle's C restatement
+    (kind "port").  Returns (checker, kind, note, oracle checker); the oracle
+    also undistorts the images beforehand (the reference has no
+    undistortion), outside every timed region."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     O.build_oracle(ref=False)
     orc = O.load("oracle")
-    threads = threads or os.cpu_count() or 1
-    W, H = sc.ref.camera.width, sc.ref.camera.height
-    cols = min(cols, W)
-    rows = min(H, 16 * threads)
-    cams = [sc.ref.camera] + [s.camera for s in sc.sources]
-    und = [c.undistorted() for c in cams]
-    imgs = [np.clip(np.round(orc.undistort(im, c.intrinsics_array())), 0, 255).astype(np.uint8)
-            for im, c in zip([sc.ref.image] + [s.image for s in sc.sources], cams)]
-    x0 = W // 2 - cols // 2
+    if O.reference_tree() is not None or os.path.exists(O.REF_SO):
+        try:
+            O.build_oracle(ref=True)
+            return (O.load("reference_release"), "reference",
+                    "the reference's own patchmatch_stereo.cpp (release flags -O3 -DNDEBUG)", orc)
+        except Exception as e:  # noqa: BLE001 -- a failed build falls back, and says so
+            return orc, "port", f"oracle restatement (reference build failed: {str(e)[:120]})", orc
+    return orc, "port", "oracle restatement of patchmatch_stereo.cpp (no reference sources on this host)", orc
 
-    def crop(nrows):
-        y0 = H // 2 - nrows // 2
-        cr = copy.deepcopy(und[0])
-        cr.cx, cr.cy = und[0].cx - x0, und[0].cy - y0
-        cr.width, cr.height = cols, nrows
-        ref = np.ascontiguousarray(imgs[0][y0:y0 + nrows, x0:x0 + cols])
-        return O.ViewSet(ref, imgs[1:], cr, und[1:])
 
-    def cfg(iters):
-        return O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=iters, patch_size=K,
-                             num_threads=threads, subpixel_iterations=4)
+class CpuReferenceSampler:
+    """Times the reference's PatchMatchStereo + RefineSubpixel on bounded
+    samples of one depth map and extrapolates to the whole map.
 
-    vs = crop(rows)
-    t0 = time.perf_counter()
-    orc.patchmatch_stereo(vs, cfg(0))
-    t_init = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    pm = orc.patchmatch_stereo(vs, cfg(1))
-    t_one = max(0.0, time.perf_counter() - t0 - t_init)
-    vs_r = crop(refine_rows)
-    r0 = rows // 2 - refine_rows // 2
-    pm_r = type(pm)(pm.filled, np.ascontiguousarray(pm.depth[r0:r0 + refine_rows]),
-                    np.ascontiguousarray(pm.support[r0:r0 + refine_rows]),
-                    np.ascontiguousarray(pm.confidence[r0:r0 + refine_rows]))
-    t0 = time.perf_counter()
-    orc.refine_subpixel(vs_r, cfg(1), pm_r)
-    t_ref = time.perf_counter() - t0
-    area = (W * H) / (cols * rows)
-    total = (t_init + ITERS * t_one) * area + t_ref * (W * H) / (cols * refine_rows)
-    note = (f"reference algorithm (oracle restatement of patchmatch_stereo.cpp), {threads} threads: initial cost + "
-            f"1 iteration on a centred {cols}x{rows} crop, scaled x{ITERS} iterations and x{area:.1f} to the frame; "
-            f"single-threaded RefineSubpixel on {cols}x{refine_rows}, scaled to the frame; "
-            f"{t_init + t_one + t_ref:.1f} s measured")
-    return total, threads, note
+    The frame is cut into a grid of tiles, `cols` wide and 16 x threads rows
+    tall (the reference splits each sweep into min(threads, H/16) row blocks,
+    so every thread stays busy); the last tile of a row or column is moved
+    inwards so that the grid covers the frame.  One sample = one tile:
+    PatchMatchStereo with 0 iterations (initial cost) and with 1 iteration,
+    whose difference is one iteration (4 direction sweeps); then
+    RefineSubpixel (single-threaded in the reference) on `refine_rows` rows
+    at the tile's middle.  Per-map estimate of a sample = (initial + ITERS x
+    one iteration) x frame / tile area + refine x frame / refined area.
+    Samples visit the tiles in a fixed shuffled order, so consecutive samples
+    spread over the frame (borders, weak-texture patches, occlusions)."""
+
+    def __init__(self, sc, threads=None, cols=480, refine_rows=4):
+        import numpy as np
+
+        self.chk, self.kind, self.impl_note, orc = cpu_reference_impl()
+        import oracle as O
+
+        self.O = O
+        self.threads = threads or os.cpu_count() or 1
+        self.sc = sc
+        self.W, self.H = sc.ref.camera.width, sc.ref.camera.height
+        self.cols = min(cols, self.W)
+        self.rows = min(self.H, 16 * self.threads)
+        self.refine_rows = refine_rows
+        cams = [sc.ref.camera] + [s.camera for s in sc.sources]
+        self.und = [c.undistorted() for c in cams]
+        self.imgs = [np.clip(np.round(orc.undistort(im, c.intrinsics_array())), 0, 255).astype(np.uint8)
+                     for im, c in zip([sc.ref.image] + [s.image for s in sc.sources], cams)]
+
+        def starts(n, size):
+            v = list(range(0, n - size + 1, size))
+            if v[-1] + size < n:
+                v.append(n - size)
+            return v
+
+        grid = [(x, y) for y in starts(self.H, self.rows) for x in starts(self.W, self.cols)]
+        self.tiles = [grid[i] for i in np.random.default_rng(0).permutation(len(grid))]
+
+    def _cfg(self, iters, threads=None):
+        sc = self.sc
+        return self.O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=iters,
+                                  patch_size=K, num_threads=threads or self.threads, subpixel_iterations=4)
+
+    def _views(self, x0, y0, cols, rows):
+        import copy
+
+        import numpy as np
+
+        cr = copy.deepcopy(self.und[0])
+        cr.cx, cr.cy = self.und[0].cx - x0, self.und[0].cy - y0
+        cr.width, cr.height = cols, rows
+        ref = np.ascontiguousarray(self.imgs[0][y0:y0 + rows, x0:x0 + cols])
+        return self.O.ViewSet(ref, self.imgs[1:], cr, self.und[1:])
+
+    def sample(self, i):
+        """Sample i: (measured seconds, per-map estimate in seconds)."""
+        import numpy as np
+
+        x0, y0 = self.tiles[i % len(self.tiles)]
+        vs = self._views(x0, y0, self.cols, self.rows)
+        t0 = time.perf_counter()
+        self.chk.patchmatch_stereo(vs, self._cfg(0))
+        t_init = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        pm = self.chk.patchmatch_stereo(vs, self._cfg(1))
+        t_pm1 = time.perf_counter() - t0
+        t_one = max(0.0, t_pm1 - t_init)
+        r0 = self.rows // 2 - self.refine_rows // 2
+        vs_r = self._views(x0, y0 + r0, self.cols, self.refine_rows)
+        pm_r = type(pm)(pm.filled, np.ascontiguousarray(pm.depth[r0:r0 + self.refine_rows]),
+                        np.ascontiguousarray(pm.support[r0:r0 + self.refine_rows]),
+                        np.ascontiguousarray(pm.confidence[r0:r0 + self.refine_rows]))
+        t0 = time.perf_counter()
+        self.chk.refine_subpixel(vs_r, self._cfg(1), pm_r)
+        t_ref = time.perf_counter() - t0
+        area = self.W * self.H / (self.cols * self.rows)
+        est = (t_init + ITERS * t_one) * area + t_ref * self.W * self.H / (self.cols * self.refine_rows)
+        return t_init + t_pm1 + t_ref, est
+
+    def full_map(self):
+        """The whole map once, no extrapolation: (PatchMatchStereo seconds,
+        RefineSubpixel seconds, filled pixels)."""
+        vs = self._views(0, 0, self.W, self.H)
+        t0 = time.perf_counter()
+        pm = self.chk.patchmatch_stereo(vs, self._cfg(ITERS))
+        t_pm = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        self.chk.refine_subpixel(vs, self._cfg(ITERS), pm)
+        t_ref = time.perf_counter() - t0
+        return t_pm, t_ref, int(pm.filled)
+
+    def describe(self, n, measured_s):
+        return (f"{self.impl_note} ({self.kind}), {self.threads} threads, on map 0 of the workload: {n} "
+                f"sample(s) of a {self.cols}x{self.rows} tile each (initial cost + 1 iteration, RefineSubpixel "
+                f"single-threaded on {self.cols}x{self.refine_rows}), tiles from a {len(self.tiles)}-tile grid "
+                f"covering the frame in a fixed shuffled order, each scaled to {ITERS} iterations and the "
+                f"{self.W}x{self.H} frame; {measured_s:.1f} s measured")
+
+
+def cpu_baseline_sample(sc, n_samples=4):
+    """cpu_baseline of the GPU arm: a bounded sample (n_samples tiles, about
+    10-30 s of CPU work) of map 0.  Returns (seconds per map, threads, kind,
+    note)."""
+    smp = CpuReferenceSampler(sc)
+    runs = [smp.sample(i) for i in range(n_samples)]
+    est = statistics.mean(r[1] for r in runs)
+    return est, smp.threads, smp.kind, smp.describe(n_samples, sum(r[0] for r in runs))
 
 
 def describe_workload(scenes):
@@ -268,30 +343,49 @@ def describe_workload(scenes):
 
 
 def run_reference_arm(args):
+    """The reference's own CPU implementation on the host cores.  A step is
+    one bounded sample (one tile of map 0, see CpuReferenceSampler); value =
+    1 / the mean per-map estimate of the timed steps, ms_per_step = the
+    measured time of a sample.  --full-map instead times the whole map 0
+    once (no extrapolation) and reports every tile's estimate beside it."""
     world, rank, _ = dist_init()
     if rank != 0:
         return
     scenes = make_scenes("cpu")
-    sc = scenes[0]
-    secs = []
-    threads = os.cpu_count() or 1
-    note = ""
+    smp = CpuReferenceSampler(scenes[0])
+    if args.full_map:
+        t_pm, t_ref, filled = smp.full_map()
+        runs = [smp.sample(i) for i in range(len(smp.tiles))]
+        est = statistics.mean(r[1] for r in runs)
+        full = t_pm + t_ref
+        print(json.dumps({"impl": "reference", "kind": smp.kind, "threads": smp.threads,
+                          "workload": f"{describe_workload(scenes)}; {K}x{K}, {ITERS} iterations; map 0",
+                          "full_map_s": full, "patchmatch_s": t_pm, "refine_s": t_ref, "filled": filled,
+                          "tile_estimate_s": est, "tiles": len(runs),
+                          "tile_estimate_rel_err": (est - full) / full,
+                          "first_k_estimates": {str(k): statistics.mean(r[1] for r in runs[:k])
+                                                for k in (4, 10, 20) if k <= len(runs)}}))
+        return
+    runs = []
     for i in range(args.warmup + args.steps):
-        t, threads, note = cpu_reference_sample(sc)
+        r = smp.sample(i)
         if i >= args.warmup:
-            secs.append(t)
-    per_map = statistics.mean(secs)
+            runs.append(r)
+    per_map = statistics.mean(r[1] for r in runs)
     value = 1.0 / per_map
+    measured = sum(r[0] for r in runs)
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": per_map * 1000.0, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scenes, analytic truth)",
+            "warmup": args.warmup, "ms_per_step": measured / len(runs) * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scenes, analytic truth)",
             "impl": "reference",
             "config": {"workload": f"{describe_workload(scenes)}; {K}x{K}, {ITERS} iterations",
-                       "algorithm": "the reference's PatchMatchStereo + RefineSubpixel (FP64, host threads), "
-                                    "timed per depth map on map 0 of the workload",
+                       "algorithm": "the reference's PatchMatchStereo + RefineSubpixel (FP64, host threads); a "
+                                    "step is one tile sample of map 0, value extrapolates the samples to "
+                                    "whole depth maps",
+                       "seconds_per_map_estimate": per_map,
                        "parallelism": "host threads"},
-            "cpu_baseline": {"value": value, "unit": "depth maps/s", "cores": threads, "kind": "port",
-                             "sample": note},
+            "cpu_baseline": {"value": value, "unit": "depth maps/s", "cores": smp.threads, "kind": smp.kind,
+                             "sample": smp.describe(len(runs), measured)},
             "e2e": {"value": value, "unit": "depth maps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -640,8 +734,8 @@ def run_gpu(args):
         ra["chosen_same_map"] = accuracy(maps[:1], truths[:1])
         line["reference_algorithm"] = ra
     if rank == 0 and not args.no_cpu_baseline:
-        secs, threads, note = cpu_reference_sample(scenes[0])
-        line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": "port",
+        secs, threads, kind, note = cpu_baseline_sample(scenes[0])
+        line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": kind,
                                 "sample": note}
     if rank == 0:
         print(json.dumps(line))
@@ -948,6 +1042,8 @@ def main():
     ap.add_argument("--interp", type=int, default=None, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--full-map", action="store_true",
+                    help="with --impl reference: time the whole map 0 once and every tile sample beside it")
     ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3", "c4", "c5"])
     ap.add_argument("--no-fusion", action="store_true", help="skip the capture's consistency + fusion stage")
     ap.add_argument("--no-reference-map", action="store_true",

@@ -4,8 +4,8 @@ Two libraries share one ABI (oracle/mvs_oracle.h):
   * liboracle.so        -- the C restatement of the reference MVS path
                            (oracle/mvs_oracle.c), built here and on any host;
   * _ref/libref_mvs.so  -- the reference's own sources compiled as they are
-                           (oracle/ref_wrapper.cpp), only where the reference
-                           tree is present.
+                           (oracle/ref_wrapper.cpp), where the reference tree
+                           or its staged copy (oracle/_ref/tree) is present.
 
 Only tests/, __graft_entry__.smoke() and bench.py (CPU baseline and the
 reference arm) may import this module.  The GPU engine never does.
@@ -22,7 +22,20 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_mvs.so")
-REFERENCE_TREE = "/root/reference"
+REF_RELEASE_SO = os.path.join(HERE, "_ref", "libref_mvs_release.so")
+# The reference project's tree: $RECON_REFERENCE_TREE when set, else the
+# staged copy of the few files this path needs (`make -C oracle stage`, made
+# where the reference exists; git-ignored, it travels with the working tree).
+STAGED_TREE = os.path.join(HERE, "_ref", "tree")
+
+
+def reference_tree() -> str | None:
+    env = os.environ.get("RECON_REFERENCE_TREE")
+    if env and os.path.isdir(env):
+        return env
+    if os.path.isfile(os.path.join(STAGED_TREE, "core", "src", "mvs", "patchmatch_stereo.cpp")):
+        return STAGED_TREE
+    return None
 
 
 class Intrinsics(C.Structure):
@@ -167,7 +180,9 @@ def build_oracle(ref: bool | None = None, quiet=True) -> None:
     """Compile liboracle.so (and the reference library when the reference
     tree exists and `ref` is not False)."""
     targets = ["all"]
-    if ref or (ref is None and os.path.isdir(REFERENCE_TREE)):
+    if os.environ.get("RECON_REFERENCE_TREE"):
+        targets.append("stage")
+    if ref or (ref is None and reference_tree() is not None):
         targets.append("ref")
     subprocess.run(["make", "-s", "-C", HERE, *targets], check=True,
                    stdout=subprocess.DEVNULL if quiet else None)
@@ -199,13 +214,15 @@ def _bind(lib: C.CDLL, prefix: str):
 
 
 def load(which: str = "oracle") -> "Checker":
-    """which = 'oracle' (the C restatement) or 'reference' (the reference's
-    own sources)."""
+    """which = 'oracle' (the C restatement), 'reference' (the reference's
+    own sources, built to pin the restatement bit for bit) or
+    'reference_release' (the same sources with the reference's release
+    flags: what the CPU baseline times)."""
     if which in _LIBS:
         return _LIBS[which]
-    path = ORACLE_SO if which == "oracle" else REF_SO
+    path = {"oracle": ORACLE_SO, "reference": REF_SO, "reference_release": REF_RELEASE_SO}[which]
     if not os.path.exists(path):
-        build_oracle(ref=(which == "reference"))
+        build_oracle(ref=(which != "oracle"))
     lib = C.CDLL(path)
     prefix = "orc_" if which == "oracle" else "ref_"
     _bind(lib, prefix)
@@ -255,7 +272,7 @@ def load(which: str = "oracle") -> "Checker":
 
 
 def reference_available() -> bool:
-    return os.path.exists(REF_SO) or os.path.isdir(REFERENCE_TREE)
+    return os.path.exists(REF_SO) or reference_tree() is not None
 
 
 @dataclass

@@ -28,7 +28,7 @@ def orc():
 def ref_lib():
     import oracle
 
-    if not os.path.isdir(oracle.REFERENCE_TREE) and not os.path.exists(oracle.REF_SO):
+    if oracle.reference_tree() is None and not os.path.exists(oracle.REF_SO):
         pytest.skip("reference tree not present on this host")
     oracle.build_oracle(ref=True)
     return oracle.load("reference")

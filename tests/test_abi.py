@@ -101,20 +101,12 @@ def test_select_source_views_matches_oracle(M, orc):
 def test_reference_binding_links():
     """The reference-side binding replaces patchmatch_stereo.cpp: it compiles
     against the reference's own headers and the reference's unmodified unit
-    test links against it and the engine library."""
-    ref = O.REFERENCE_TREE
-    if not os.path.isdir(ref):
-        pytest.skip("reference tree not present")
-    import recon_mvs
+    test links against it and the engine library (it runs on the GPU in
+    test_gpu_reference_unit.py)."""
+    import ref_unit
 
-    lib = recon_mvs.LIB_PATH
-    recon_mvs.load_library()
-    shim = os.path.join(ROOT, "recon-scanner_gb300", "bindings", "patchmatch_stereo_gb300.cpp")
-    out = os.path.join(ROOT, "recon-scanner_gb300", "_build", "test_mvs_gb300")
-    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ref, "core", "include"), "-I", os.path.join(ROOT, "include"),
-           os.path.join(ref, "tests", "unit", "test_mvs.cpp"), shim, os.path.join(ref, "core", "src", "util", "camera.cpp"),
-           os.path.join(ref, "core", "src", "util", "linalg.cpp"), lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", out]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-2000:]
+    out = ref_unit.build_reference_unit_test()
+    if out is None:
+        pytest.skip("reference tree not present")
     syms = subprocess.run(["nm", "-C", out], capture_output=True, text=True).stdout
     assert "recon::PatchMatchStereo" in syms and "recon_mvs_patchmatch" in syms
