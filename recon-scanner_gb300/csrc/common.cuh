@@ -153,9 +153,11 @@ struct SrcView {
   ff Aff[9];  // A in float-float (per-pixel source rays without FP64)
 };
 
-// Columns of one reference-tile plane staged by a sweep block: the warp's 32
-// same-colour pixels + 8 margin each side (a TMA box row of 192 bytes).
-constexpr int kTileCols = 48;
+// Columns of one reference-tile plane staged by a sweep block: the tile's 32
+// same-colour column pairs, 8 margin on the left and 16 on the right (a TMA
+// box row of 224 bytes).  The row pitch of 56 words puts the 4 rows x 8
+// consecutive pairs that one warp reads into 32 distinct banks.
+constexpr int kTileCols = 56;
 
 // Source read modes of the plane-mode kernels (Job::src_mode).
 constexpr int kSrcExact = 0, kSrcTex = 1, kSrcBf16 = 2;

@@ -304,8 +304,9 @@ struct GlobalRef {
 };
 
 // Shared-memory tile of the reference image stored as even / odd column
-// planes, so that the 32 lanes of a warp (32 same-colour pixels of one row,
-// two columns apart) read consecutive words: conflict-free.
+// planes, so that the lanes of a warp (same-colour pixels two columns apart,
+// 8 per row in 4 rows) read consecutive words of 4 rows whose pitch puts them
+// in distinct banks: conflict-free.
 
 struct TileRow {
   const float* a;
@@ -317,10 +318,10 @@ struct TileRow {
 struct TileRef {
   const float* same;   // the column plane of this thread's own parity, [rows][kTileCols]
   const float* other;  // the other plane
-  int lane, parity, ty;
+  int pair, parity, ty;  // the pixel's column pair and row in the tile
   template <int H>
   __device__ __forceinline__ TileRow row(int dy) const {
-    const int r = (ty + H + dy) * kTileCols + lane + 8;
+    const int r = (ty + H + dy) * kTileCols + pair + 8;
     if (H & 1) return TileRow{other + r + parity - (H + 1) / 2, same + r - (H - 1) / 2};
     return TileRow{same + r - H / 2, other + r + parity - H / 2};
   }

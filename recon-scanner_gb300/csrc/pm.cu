@@ -564,9 +564,15 @@ constexpr int kTmaWaitPolls = 1 << 22;
 // resident blocks) whose blocks pull work items -- 64-column x R-row tiles,
 // R = blockDim.y -- from an atomic counter until the batch is exhausted.  A
 // block of 32 x R threads owns the 32 same-colour pixels of each of its R
-// rows; the reference rows the tile reads (R + 2H rows, the 64 columns +- 16)
-// are staged once into shared memory as even / odd column planes from the
-// de-interleaved reference copy.  `queue` is this launch's work counter
+// rows; the reference rows the tile reads (R + 2H rows, the 64 columns, 16
+// more on the left and 32 on the right) are staged once into shared memory as
+// even / odd column planes from the de-interleaved reference copy.
+//
+// A warp owns a compact patch, not a row: RW = min(R, 4) rows x 32 / RW
+// same-colour pixels (16 x 4 pixels for R >= 4).  Each window sample of a
+// warp is one texture instruction over its 32 pixels, and their source
+// footprints then cluster in a 2-D patch of the source instead of spreading
+// along a 64-pixel row: fewer texture-cache lines per instruction.  `queue` is this launch's work counter
 // (zeroed by the init kernel); `total` its item count -- jobs with fewer
 // iterations than `iter + 1` sit at the end of the job order and fall
 // outside it.
@@ -583,6 +589,12 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const PCache pc{smem, nthreads, tid};
   const int box_rows = R + 2 * H;
+  // this thread's pixel in the tile: row ty, same-colour column pair `pair`
+  const int RW = R < 4 ? R : 4;        // rows per warp
+  const int PW = 32 / RW;              // pixels per warp row
+  const int w = (int)threadIdx.y, l = (int)threadIdx.x;
+  const int ty = (w / RW) * RW + l / PW;
+  const int pair = (w % RW) * PW + l % PW;
   if constexpr (H > 0) {
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
@@ -598,11 +610,11 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
     const int local = item - B.start[j];
     const int tiles_x = (J.w + 63) >> 6;
     const int bx = local % tiles_x, by = local / tiles_x;
-    const int y = by * R + (int)threadIdx.y;
+    const int y = by * R + ty;
     const int parity = (y + color) & 1;
-    const int x = bx * 64 + 2 * (int)threadIdx.x + parity;
+    const int x = bx * 64 + 2 * pair + parity;
     if constexpr (H > 0) {
-      // the tile: planes [2][box_rows][48] of ref_de from column bx*32 - 8 and
+      // the tile: planes [2][box_rows][kTileCols] of ref_de from column bx*32 - 8 and
       // row by*R - H, one TMA box (zeros outside the image)
       if (tid == 0)
         tma_load_3d(tile, B.tmaps + j, bx * 32 - 8, by * R - H, 0, &bar,
@@ -622,8 +634,7 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
       if constexpr (H > 0) {
         const float* plane0 = tile;
         const float* plane1 = tile + box_rows * kTileCols;
-        const TileRef ref{parity ? plane1 : plane0, parity ? plane0 : plane1, (int)threadIdx.x, parity,
-                          (int)threadIdx.y};
+        const TileRef ref{parity ? plane1 : plane0, parity ? plane0 : plane1, pair, parity, ty};
         const RefWindow rw = tile_window<H>(J, ref, x, y);
         sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
       } else {
