@@ -126,11 +126,12 @@ def make_scenes(device):
         return [Syn.sphere_on_backdrop(width=W, height=H, f=F, num_sources=S_SRC, seed=1, device=device)]
     if WORKLOAD == "c3":
         return Syn.orbit_capture(n_frames=120, n_refs=48, seed=3, device=device)
-    cap = Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device)
+    cap = Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, seed=2, device=device, depth_range=DEPTH_RANGE)
     return [Syn.as_reference(cap, k) for k in range(len(cap.views))]
 
 
 WORKLOAD = "c2"
+DEPTH_RANGE = (0.25, 0.70)  # the tabletop capture's search range: every view's depths (0.30-0.63 m)
 
 
 def set_workload(name):
@@ -302,15 +303,20 @@ class CpuReferenceSampler:
 
     def full_map(self):
         """The whole map once, no extrapolation: (PatchMatchStereo seconds,
-        RefineSubpixel seconds, filled pixels)."""
+        RefineSubpixel seconds, the refined map's accuracy vs analytic
+        truth)."""
         vs = self._views(0, 0, self.W, self.H)
         t0 = time.perf_counter()
         pm = self.chk.patchmatch_stereo(vs, self._cfg(ITERS))
         t_pm = time.perf_counter() - t0
         t0 = time.perf_counter()
-        self.chk.refine_subpixel(vs, self._cfg(ITERS), pm)
+        refined = self.chk.refine_subpixel(vs, self._cfg(ITERS), pm)
         t_ref = time.perf_counter() - t0
-        return t_pm, t_ref, int(pm.filled)
+
+        class _Map:
+            depth = refined.depth
+
+        return t_pm, t_ref, accuracy([_Map], [self.sc.ref.depth], (self.sc.min_depth, self.sc.max_depth))
 
     def describe(self, n, measured_s):
         return (f"{self.impl_note} ({self.kind}), {self.threads} threads, on map 0 of the workload: {n} "
@@ -354,13 +360,13 @@ def run_reference_arm(args):
     scenes = make_scenes("cpu")
     smp = CpuReferenceSampler(scenes[0])
     if args.full_map:
-        t_pm, t_ref, filled = smp.full_map()
+        t_pm, t_ref, acc = smp.full_map()
         runs = [smp.sample(i) for i in range(len(smp.tiles))]
         est = statistics.mean(r[1] for r in runs)
         full = t_pm + t_ref
         print(json.dumps({"impl": "reference", "kind": smp.kind, "threads": smp.threads,
                           "workload": f"{describe_workload(scenes)}; {K}x{K}, {ITERS} iterations; map 0",
-                          "full_map_s": full, "patchmatch_s": t_pm, "refine_s": t_ref, "filled": filled,
+                          "full_map_s": full, "patchmatch_s": t_pm, "refine_s": t_ref, "accuracy": acc,
                           "tile_estimate_s": est, "tiles": len(runs),
                           "tile_estimate_rel_err": (est - full) / full,
                           "first_k_estimates": {str(k): statistics.mean(r[1] for r in runs[:k])
@@ -460,11 +466,14 @@ class _Null:
         return False
 
 
-def accuracy(maps, truths):
-    """Pooled over the step's maps: relative depth error vs analytic truth."""
+def accuracy(maps, truths, depth_range=None):
+    """Pooled over the step's maps: relative depth error vs analytic truth.
+    With the search range given, also over the pixels whose true depth lies
+    inside it (no search can return a depth outside its range), and the
+    share of pixels whose truth lies outside."""
     import numpy as np
 
-    rel_all, abs_all, filled = [], [], []
+    rel_all, abs_all, filled, rel_in, outside = [], [], [], [], []
     for dm, truth in zip(maps, truths):
         err = np.abs(dm.depth.astype(np.float64) - truth)
         rel = err / truth
@@ -472,12 +481,24 @@ def accuracy(maps, truths):
         rel_all.append(rel[ok])
         abs_all.append(err[ok])
         filled.append(float(np.isfinite(dm.depth).mean()))
+        if depth_range is not None:
+            with np.errstate(invalid="ignore"):
+                inside = (truth >= depth_range[0]) & (truth <= depth_range[1])
+            rel_in.append(rel[ok & inside])
+            outside.append(float((np.isfinite(truth) & ~inside).sum()) / max(1, int(np.isfinite(truth).sum())))
     rel = np.concatenate(rel_all) if rel_all else np.zeros(0)
     err = np.concatenate(abs_all) if abs_all else np.zeros(0)
-    return {"filled": float(np.mean(filled)),
-            "median_rel_err": float(np.median(rel)) if rel.size else None,
-            "p95_rel_err": float(np.quantile(rel, 0.95)) if rel.size else None,
-            "median_abs_err_mm": float(np.median(err) * 1e3) if err.size else None}
+    out = {"filled": float(np.mean(filled)),
+           "median_rel_err": float(np.median(rel)) if rel.size else None,
+           "p95_rel_err": float(np.quantile(rel, 0.95)) if rel.size else None,
+           "median_abs_err_mm": float(np.median(err) * 1e3) if err.size else None}
+    if depth_range is not None:
+        r = np.concatenate(rel_in) if rel_in else np.zeros(0)
+        out["in_range"] = {"median_rel_err": float(np.median(r)) if r.size else None,
+                           "p95_rel_err": float(np.quantile(r, 0.95)) if r.size else None,
+                           "truth_outside_range": float(np.mean(outside)),
+                           "per_map_truth_outside_range": [round(v, 4) for v in outside]}
+    return out
 
 
 def agreement(maps_a, maps_b):
@@ -531,27 +552,45 @@ def fuse_capture(M, scenes, maps, rel=0.01, reproj=1.0, min_views=3):
             "timing": "host wall clock: 9 consistency calls + fusion, host buffers in and out"}
 
 
-def reference_algorithm_map(M, sc, cfg):
-    """The reference's own algorithm on one map of the workload:
+def reference_algorithm_maps(M, scenes, cfgs, maps):
+    """The reference's own algorithm on every map of the workload:
     PatchMatchStereo + RefineSubpixel (fronto-parallel windows, golden
     section + parabola fit; patchmatch_stereo.cpp:422-979) run by the
     engine's COMPAT mode, its device restatement, on the views undistorted on
     the device and rounded to 8 bits (the reference's input type), with
-    pinhole cameras.  Returns its accuracy vs analytic truth and its time."""
+    pinhole cameras.  Per map: its accuracy vs analytic truth next to the
+    chosen form's on the same map (all pixels, and the pixels whose true
+    depth lies in the search range); pooled; time per map."""
     import numpy as np
 
-    vs = [sc.ref] + list(sc.sources)
-    imgs = [np.clip(np.rint(M.Undistort(v.image, v.camera.intrinsics_array())), 0, 255).astype(np.uint8) for v in vs]
-    cams = [v.camera.undistorted() for v in vs]
-    va = M.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    per_map, ref_maps, secs = [], [], 0.0
     opts = M.Options(mode=M.MODE_COMPAT, device=0)
-    t0 = time.perf_counter()
-    dm = M.PatchMatchStereo(va, cfg, options=opts)
-    M.RefineSubpixel(va, cfg, dm, options=opts)
-    secs = time.perf_counter() - t0
-    out = accuracy([dm], [sc.ref.depth])
-    out["seconds"] = secs
-    out["note"] = "map 0 only; COMPAT mode = the reference's PatchMatchStereo + RefineSubpixel restated on the device"
+    for k, (sc, cfg) in enumerate(zip(scenes, cfgs)):
+        vs = [sc.ref] + list(sc.sources)
+        imgs = [np.clip(np.rint(M.Undistort(v.image, v.camera.intrinsics_array())), 0, 255).astype(np.uint8)
+                for v in vs]
+        cams = [v.camera.undistorted() for v in vs]
+        va = M.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+        t0 = time.perf_counter()
+        dm = M.PatchMatchStereo(va, cfg, options=opts)
+        M.RefineSubpixel(va, cfg, dm, options=opts)
+        secs += time.perf_counter() - t0
+        ref_maps.append(dm)
+        rng = (sc.min_depth, sc.max_depth)
+        r, c = accuracy([dm], [sc.ref.depth], rng), accuracy([maps[k]], [sc.ref.depth], rng)
+        per_map.append({"map": k, "reference_median": r["median_rel_err"], "reference_p95": r["p95_rel_err"],
+                        "chosen_median": c["median_rel_err"], "chosen_p95": c["p95_rel_err"],
+                        "reference_in_range_median": r["in_range"]["median_rel_err"],
+                        "reference_in_range_p95": r["in_range"]["p95_rel_err"],
+                        "chosen_in_range_median": c["in_range"]["median_rel_err"],
+                        "chosen_in_range_p95": c["in_range"]["p95_rel_err"],
+                        "truth_outside_range": r["in_range"]["truth_outside_range"]})
+    rng = (scenes[0].min_depth, scenes[0].max_depth)
+    out = accuracy(ref_maps, [sc.ref.depth for sc in scenes], rng)
+    out["seconds_per_map"] = secs / len(scenes)
+    out["per_map"] = per_map
+    out["note"] = ("COMPAT mode = the reference's PatchMatchStereo + RefineSubpixel restated on the device; "
+                   "in_range = pixels whose true depth lies in the search range")
     return out
 
 
@@ -611,7 +650,9 @@ def run_gpu(args):
                                                                      flush, world, undistort, clk, scenes=scenes)
     total_ms = barrier_max(world, float(sum(step_ms)))
     value = world * n_maps * args.steps / (total_ms / 1000.0)
-    acc = accuracy(maps, truths)
+    rng = {(sc.min_depth, sc.max_depth) for sc in scenes}
+    rng = rng.pop() if len(rng) == 1 else None
+    acc = accuracy(maps, truths, rng)
 
     plain = None
     if not args.plain and not args.chosen_only:
@@ -625,7 +666,7 @@ def run_gpu(args):
                  "ms_per_step": p_total / args.steps, "storage": "fp16" if p_fp16 else "fp32",
                  "interp": "texture-unit" if p_interp else "exact fp32", "launch": "one launch per view",
                  "refine": "golden section on the inverse depth (the reference's schedule)",
-                 "gpu_launches_per_step": p_launches, "accuracy": accuracy(p_maps, truths),
+                 "gpu_launches_per_step": p_launches, "accuracy": accuracy(p_maps, truths, rng),
                  "chosen_vs_plain_median_rel_depth_diff": med, "chosen_vs_plain_p95_rel_depth_diff": p95}
 
     # ---- end to end through the C ABI from host buffers ----
@@ -730,9 +771,7 @@ def run_gpu(args):
         line["fusion"] = fuse_capture(M, scenes, maps)
         line["stage"] = stage_capture_run(M, scenes, opts)
     if WORKLOAD == "c2" and not args.no_reference_map:
-        ra = reference_algorithm_map(M, scenes[0], cfgs[0])
-        ra["chosen_same_map"] = accuracy(maps[:1], truths[:1])
-        line["reference_algorithm"] = ra
+        line["reference_algorithm"] = reference_algorithm_maps(M, scenes, cfgs, maps)
     if rank == 0 and not args.no_cpu_baseline:
         secs, threads, kind, note = cpu_baseline_sample(scenes[0])
         line["cpu_baseline"] = {"value": 1.0 / secs, "unit": "depth maps/s", "cores": threads, "kind": kind,
@@ -1047,11 +1086,15 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3", "c4", "c5"])
     ap.add_argument("--no-fusion", action="store_true", help="skip the capture's consistency + fusion stage")
     ap.add_argument("--no-reference-map", action="store_true",
-                    help="skip the reference algorithm's map (COMPAT mode) on map 0 of the capture")
+                    help="skip the reference algorithm's maps (COMPAT mode) of the capture")
     ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
     ap.add_argument("--tile-rows", type=int, default=0, help="sweep tile rows (2, 4, 8); 0 = autotuned")
+    ap.add_argument("--depth-range", default=None, help="the tabletop capture's search range 'lo,hi' in metres")
     args = ap.parse_args()
     set_workload(args.workload)
+    if args.depth_range:
+        global DEPTH_RANGE
+        DEPTH_RANGE = tuple(float(v) for v in args.depth_range.split(","))
     # the chosen form (default): FP16 storage + texture-unit interpolation;
     # the plain FP32 path is timed beside it unless --plain asks for it alone
     if args.refine is None:

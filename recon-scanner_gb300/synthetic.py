@@ -372,13 +372,15 @@ def tabletop_scene(seed: int = 2) -> Scene:
 
 def tabletop(width=1920, height=1440, f=1450.0, num_sources=8, k1=0.05, k2=-0.01,
              seed=2, device="cpu", noise_sigma=1.0 / 255.0, baseline=(0.08, 0.12),
-             arc_deg=240.0) -> MvsScene:
+             arc_deg=240.0, depth_range=(0.25, 0.70)) -> MvsScene:
     """The full-resolution workload: the tabletop scene seen from 0.375 m
     with the plane spanning about 0.3-0.5 m of depth, 8 sources on a seeded
     80-120 mm baseline arc around the reference, all with Brown-Conrady
     distortion (k1, k2); images are rendered distorted and must be
     undistorted before matching.  Truth depth refers to the undistorted
-    reference camera."""
+    reference camera.  The search range covers what every view of the
+    capture sees (0.30-0.63 m): used as references, the views on the far
+    side of the arc see the table up to 0.63 m."""
     sc = tabletop_scene(seed)
     rng = np.random.default_rng(seed + 17)
     tilt = math.radians(26.7)  # plane normal vs optical axis
@@ -397,7 +399,7 @@ def tabletop(width=1920, height=1440, f=1450.0, num_sources=8, k1=0.05, k2=-0.01
         R, t = look_at(c, target)
         cams.append(Camera(f, f, cx, cy, width, height, R, t, k1=k1, k2=k2))
     views = [render(sc, cam, noise_sigma, seed * 1000 + i, device) for i, cam in enumerate(cams)]
-    return MvsScene("tabletop", views[0], views[1:], 0.25, 0.55, seed)
+    return MvsScene("tabletop", views[0], views[1:], depth_range[0], depth_range[1], seed)
 
 
 def orbit_cameras(n_frames=120, seed=3, resolutions=((640, 480), (1280, 960), (1920, 1440)),
