@@ -59,7 +59,7 @@ W, H, F, ITERS = 1920, 1440, 1450.0, 8
 # algorithmic FLOP of the plane-induced homography cost: K^2 * 26 + 30 per
 # source window sampled (26 = 15 projection + 6 bilinear + 5 moments), 40 per
 # hypothesis
-SM_COUNT, FP32_LANES = 152, 128
+FP32_LANES = 128  # FP32 lanes per SM (sm_100 / sm_103 family)
 
 
 def load_peaks():
@@ -612,8 +612,58 @@ def stage_capture_run(M, scenes, opts):
     cloud, nmaps = eng.stage_run(*args, **kw)
     secs = time.perf_counter() - t0
     eng.close()
+    # the sources SelectSourceViews gives each keyframe inside the stage (its
+    # scale-ratio gate drops some): the stage's PatchMatch work differs from
+    # the timed step's, where every map takes the capture's other 8 views
+    poses = args[1]
+    src = [len(M.SelectSourceViews(poses[k], poses, cams[k].intrinsics_array(), cfg)) for k in range(len(cams))]
     return {"seconds": secs, "maps": nmaps, "points": int(cloud.size()), "maps_per_s": nmaps / secs,
-            "call": "recon_mvs_stage_run, host images in, fused cloud out"}
+            "call": "recon_mvs_stage_run, host images in, fused cloud out",
+            "sources_per_map": src, "source_views": int(sum(src)),
+            "value_source_views": int(sum(len(sc.sources) for sc in scenes)),
+            "refine": {0: "none", 1: "golden section", 2: "Gauss-Newton"}.get(int(opts.refine), str(opts.refine)),
+            "note": "the stage selects each keyframe's sources with SelectSourceViews (num_views = 8, scale-ratio "
+                    "gate), so it searches fewer source views than the timed step; no L2 flush between its calls"}
+
+
+KERNEL_SOURCES = ["pm.cu", "cost.cuh", "common.cuh", "adjoint.cuh", "kernels.h"]
+
+
+def kernel_sources_digest():
+    """Digest of the sweep's kernel sources: a profile taken on other
+    sources does not describe the kernel this run times."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "recon-scanner_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def sweep_profile(workload, args):
+    """The committed ncu figures of the sweep kernel for this workload and
+    form (profiles/traffic.json): DRAM bytes and texture-pipe share per
+    launch, with the commit and kernel-source digest they were taken at.
+    `applies` is true only when the digest matches these sources and the form
+    matches this run's."""
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tp):
+        return {"applies": False, "why": "no committed profile"}
+    with open(tp) as f:
+        prof = json.load(f).get("k_plane_sweep", {}).get(workload)
+    if not prof:
+        return {"applies": False, "why": f"no committed profile for workload {workload}"}
+    form = {"fp16": bool(args.fp16), "interp": int(args.interp), "per_view": bool(args.per_view)}
+    digest = kernel_sources_digest()
+    out = dict(prof)
+    out["sources_digest_now"] = digest
+    out["applies"] = prof.get("sources_digest") == digest and prof.get("form") == form
+    if prof.get("form") != form:
+        out["why"] = "profiled form differs from this run's"
+    elif prof.get("sources_digest") != digest:
+        out["why"] = "kernel sources changed since the profile"
+    return out
 
 
 def run_gpu(args):
@@ -711,15 +761,11 @@ def run_gpu(args):
     flop_per_launch = flop_per_window * win_per_launch + flop_per_hyp_setup * hyp_per_launch
     achieved_tflops = flop_per_launch / (per_launch_ms * 1e-3) / 1e12
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
-    peak_tflops = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
-    traffic, tex_pipe = None, None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            prof = json.load(f)
-        key = f"{WORKLOAD}{'_per_view' if args.per_view else ''}"
-        traffic = prof.get("plane_sweep_bytes_per_launch", {}).get(key)
-        tex_pipe = prof.get("plane_sweep_tex_data_pipe_pct", {}).get(key)
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    peak_tflops = sm_count * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+    prof = sweep_profile(WORKLOAD, args)
+    traffic = prof.get("dram_bytes_per_launch") if prof.get("applies") else None
+    tex_pipe = prof.get("tex_data_pipe_pct") if prof.get("applies") else None
 
     # the HBM side of the roofline, per half-sweep: the algorithmic bytes
     # (every map's source images + its per-pixel state read and written:
@@ -754,7 +800,7 @@ def run_gpu(args):
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved_tflops / peak_tflops, "traffic": traffic,
                          "kernel": "k_plane_sweep",
-                         "peak_source": f"{SM_COUNT} SMs x {FP32_LANES} FP32 lanes x 2 x sm_max_mhz {sm_mhz} "
+                         "peak_source": f"{sm_count} SMs (device) x {FP32_LANES} FP32 lanes x 2 x sm_max_mhz {sm_mhz} "
                                         f"({peak_src} MEASURED_PEAKS.json clock)",
                          "hypotheses_per_launch": hyp_per_launch, "windows_per_launch": win_per_launch,
                          "ms_per_launch": per_launch_ms, "flop_per_launch": flop_per_launch,
@@ -764,7 +810,8 @@ def run_gpu(args):
                          "binding_unit": {"unit": "L1TEX texture data pipe (bilinear source reads)",
                                           "pct_of_peak": tex_pipe,
                                           "source": "ncu l1tex__data_pipe_tex_wavefronts.avg."
-                                                    "pct_of_peak_sustained_elapsed, profiles/traffic.json"}},
+                                                    "pct_of_peak_sustained_elapsed"},
+                         "profile": prof},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
             "accuracy": acc, "plain": plain, "clocks": clk.summary()}
     if WORKLOAD == "c2" and not args.no_fusion:
