@@ -552,6 +552,69 @@ def fuse_capture(M, scenes, maps, rel=0.01, reproj=1.0, min_views=3):
             "timing": "host wall clock: 9 consistency calls + fusion, host buffers in and out"}
 
 
+def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truths, rng, chosen_value, chosen_maps):
+    """What each step from the plain path to the chosen form buys: the
+    capture timed (`--attr-steps` steps after one warm-up, L2 flushed between
+    steps) in the forms between them -- batched FP32 exact golden section,
+    + FP16 storage, + Gauss-Newton (the batched FP16 form with exact
+    interpolation) -- beside the plain path and the chosen form (texture-unit
+    interpolation) timed above; each with its accuracy.  And what the
+    texture unit's 8-bit filter weights cost: the plane cost of 2 x 10^4
+    seeded hypotheses on a pinhole copy of the capture's map 0, FP16 storage,
+    exact and texture-unit interpolation, against the FP64 oracle (a checker
+    run after every timed region)."""
+    import numpy as np
+
+    import synthetic as Syn
+
+    forms = [("batched_fp32_exact_golden", False, 0, 1), ("batched_fp16_exact_golden", True, 0, 1),
+             ("batched_fp16_exact_gauss_newton", True, 0, 2)]
+    out = {"steps": args.attr_steps, "forms": {}}
+    for name, fp16, interp, refine in forms:
+        ms, _, _, _, fmaps, _ = time_form(M, views, cfgs, mk(fp16, interp, False, refine), args.attr_steps, 1,
+                                          flush, world, undistort, scenes=scenes)
+        tot = barrier_max(world, float(sum(ms)))
+        med, p95 = agreement(fmaps, chosen_maps)
+        out["forms"][name] = {"value": world * len(views) * args.attr_steps / (tot / 1000.0),
+                              "accuracy": accuracy(fmaps, truths, rng),
+                              "vs_chosen_median_rel_depth_diff": med, "vs_chosen_p95_rel_depth_diff": p95}
+    out["forms"]["chosen_fp16_texture_gauss_newton"] = {"value": chosen_value}
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    orc = O.load("oracle")
+    sc = Syn.tabletop(width=W, height=H, f=F, num_sources=S_SRC, k1=0.0, k2=0.0, seed=2, device="cuda:0",
+                      depth_range=DEPTH_RANGE)
+    cams = sc.cameras
+    imgs = [v.image for v in sc.views]
+    rs = np.random.default_rng(23)
+    n = 20_000
+    px, py = rs.integers(0, W, n), rs.integers(0, H, n)
+    td, tn = sc.ref.depth[py, px], sc.ref.normal[py, px]
+    okt = np.isfinite(td)
+    inv = np.where(okt, 1.0 / np.where(okt, td, 1.0), rs.uniform(1 / sc.max_depth, 1 / sc.min_depth, n))
+    inv = (inv * (1.0 + rs.normal(0, 0.01, n))).astype(np.float32).astype(np.float64)
+    nrm = np.where(okt[:, None], tn, [0.0, 0.0, -1.0]) + rs.normal(0, 0.1, (n, 3))
+    nrm = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(np.float32).astype(np.float64)
+    cfg_d = dict(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, patch_size=K)
+    want, _, _ = orc.plane_costs(O.ViewSet(imgs[0], imgs[1:], cams[0], cams[1:]), O.make_config(**cfg_d),
+                                 args.best_k, px, py, inv, nrm)
+    va = M.ViewArgs.from_cameras(imgs[0], imgs[1:], cams[0], cams[1:])
+    cost = {}
+    for name, interp in (("fp16_exact", 0), ("fp16_texture", 1)):
+        o = M.Options(mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16, interp=interp, device=0)
+        got, _ = M.Evaluate(va, M.MvsConfig(**cfg_d), o, px, py, inv, nrm.astype(np.float32))
+        ok = (want < 1e29) & (got < 1e29)
+        d = np.abs(got[ok].astype(np.float64) - want[ok])
+        cost[name] = {"hypotheses": int(ok.sum()), "median_abs": float(np.median(d)),
+                      "p99_abs": float(np.quantile(d, 0.99)), "max_abs": float(d.max()),
+                      "within_1e-5_rel_plus_2e-6": float(np.mean(d <= 1e-5 * np.abs(want[ok]) + 2e-6))}
+    out["cost_vs_fp64_oracle"] = cost
+    out["note"] = ("plain = FP32 storage, exact interpolation, one launch per view, golden section; each form adds "
+                   "one change; chosen = batched, FP16, Gauss-Newton, texture-unit interpolation (8-bit weights)")
+    return out
+
+
 def reference_algorithm_maps(M, scenes, cfgs, maps):
     """The reference's own algorithm on every map of the workload:
     PatchMatchStereo + RefineSubpixel (fronto-parallel windows, golden
@@ -814,6 +877,9 @@ def run_gpu(args):
                          "profile": prof},
             "hypotheses_per_s": statistics.mean(hyps) / (statistics.mean(step_ms) * 1e-3),
             "accuracy": acc, "plain": plain, "clocks": clk.summary()}
+    if WORKLOAD == "c2" and not args.plain and not args.chosen_only and not args.no_attribution:
+        line["attribution"] = attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truths, rng,
+                                          value, maps)
     if WORKLOAD == "c2" and not args.no_fusion:
         line["fusion"] = fuse_capture(M, scenes, maps)
         line["stage"] = stage_capture_run(M, scenes, opts)
@@ -1132,6 +1198,8 @@ def main():
                     help="with --impl reference: time the whole map 0 once and every tile sample beside it")
     ap.add_argument("--workload", default="c2", choices=["c2", "small", "c3", "c4", "c5"])
     ap.add_argument("--no-fusion", action="store_true", help="skip the capture's consistency + fusion stage")
+    ap.add_argument("--no-attribution", action="store_true", help="skip timing the forms between plain and chosen")
+    ap.add_argument("--attr-steps", type=int, default=2, help="timed steps of each attribution form")
     ap.add_argument("--no-reference-map", action="store_true",
                     help="skip the reference algorithm's maps (COMPAT mode) of the capture")
     ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
