@@ -1175,6 +1175,7 @@ static orc_plane_result plane_cost_core(const orc_views* v, const orc_config* cf
     for (int i = 0; i < 3; ++i) Xs0[i] += b[i];
     if (Xs0[2] <= 1e-6) continue;
     double sr = 0, ss = 0, srr = 0, sss = 0, srs = 0;
+    double edge = 1e30;
     int valid = 0;
     for (int dy = -half; dy <= half; ++dy) {
       for (int dx = -half; dx <= half; ++dx) {
@@ -1203,6 +1204,14 @@ static orc_plane_result plane_cost_core(const orc_views* v, const orc_config* cf
         const double sv = ks->fy * (Xs[1] / Xs[2]) + ks->cy;
         double vs = 0.0;
         if (!sample_source(v, k, su, sv, half_pixel, &vs)) continue;
+        {
+          const double o = half_pixel ? 0.0 : 0.5;
+          const double fu = (su - o) - floor(su - o), fv = (sv - o) - floor(sv - o);
+          double e = fu < 1.0 - fu ? fu : 1.0 - fu;
+          if (fv < e) e = fv;
+          if (1.0 - fv < e) e = 1.0 - fv;
+          if (e < edge) edge = e;
+        }
         sr += vr;
         ss += vs;
         srr += vr * vr;
@@ -1223,6 +1232,7 @@ static orc_plane_result plane_cost_core(const orc_views* v, const orc_config* cf
     if (ncc > 1.0) ncc = 1.0;
     res.view_cost[k] = 1.0 - ncc;
     res.view_valid[k] = 1;
+    res.view_edge[k] = edge;
     vcost[nvalid++] = 1.0 - ncc;
   }
   res.valid_views = nvalid;
@@ -1295,6 +1305,32 @@ void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, 
   for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
   free(th);
   free(tasks);
+}
+
+void orc_plane_edge_distance(const orc_views* v, const orc_config* cfg, int32_t best_k, int32_t n,
+                             const int32_t* px, const int32_t* py, const double* inv,
+                             const double* normals, double* out_dist) {
+  const int nsrc = v->num_src < 32 ? v->num_src : 32;
+  for (int32_t h = 0; h < n; ++h) {
+    const orc_plane_result r =
+        plane_cost_core(v, cfg, best_k, px[h], py[h], inv[h], &normals[3 * h], 0, 1e300);
+    /* the views the cost averages: the best_k lowest view costs */
+    int order[32], m = 0;
+    for (int k = 0; k < nsrc; ++k) {
+      if (!r.view_valid[k]) continue;
+      int q = m++;
+      while (q > 0 && r.view_cost[order[q - 1]] > r.view_cost[k]) {
+        order[q] = order[q - 1];
+        --q;
+      }
+      order[q] = k;
+    }
+    const int kk = best_k > 0 && best_k < m ? best_k : m;
+    double d = 1e30;
+    for (int i = 0; i < kk; ++i)
+      if (r.view_edge[order[i]] < d) d = r.view_edge[order[i]];
+    out_dist[h] = d;
+  }
 }
 
 /* ------------------------------------------------------------------------ */

@@ -202,6 +202,7 @@ typedef struct orc_plane_result {
   int32_t valid_views;
   double view_cost[32];
   int32_t view_valid[32];
+  double view_edge[32]; /* per valid view: the smallest distance of a window sample to a texel edge */
 } orc_plane_result;
 /* half_pixel = 1 selects the reference's sampling convention instead: the
  * reference window sampled at (x+0.5+dx, y+0.5+dy) with index == coordinate
@@ -214,6 +215,14 @@ void orc_plane_costs(const orc_views* v, const orc_config* cfg, int32_t best_k, 
                      const int32_t* px, const int32_t* py, const double* inv,
                      const double* normals, double* out_cost, int32_t* out_valid_views,
                      double* out_view_cost, int32_t half_pixel);
+/* Per hypothesis: the smallest distance, in texels, from a window sample of
+ * the views the cost averages (the best_k lowest) to a texel edge of the
+ * source image -- where bilinear interpolation has a kink, so the cost is not
+ * differentiable there, and two evaluations whose sample positions differ by
+ * rounding may fall on opposite sides (pixel-centre windows). */
+void orc_plane_edge_distance(const orc_views* v, const orc_config* cfg, int32_t best_k, int32_t n,
+                             const int32_t* px, const int32_t* py, const double* inv,
+                             const double* normals, double* out_dist);
 
 /* Plane-mode PatchMatch with every cost in FP64 (orc_plane_cost, pixel-centre
  * windows): the GPU engine's red-black search -- 8 adaptive propagation

@@ -243,6 +243,7 @@ def load(which: str = "oracle") -> "Checker":
                                             P, C.c_int64, C.POINTER(C.c_int64), d, d, C.POINTER(C.c_float),
                                             C.POINTER(C.c_uint32)]
         lib.orc_plane_costs.argtypes = [V, P, C.c_int32, C.c_int32, i32, i32, d, d, d, i32, d, C.c_int32]
+        lib.orc_plane_edge_distance.argtypes = [V, P, C.c_int32, C.c_int32, i32, i32, d, d, d]
         lib.orc_geo_consistency.argtypes = [C.POINTER(DepthMapC), C.c_int32, C.POINTER(Pose), C.POINTER(Intrinsics),
                                             C.c_int32, C.POINTER(ConsistencyParams), C.POINTER(C.c_uint8),
                                             C.POINTER(C.c_uint8)]
@@ -396,6 +397,19 @@ class Checker:
                                    _ptr(px, C.c_int32), _ptr(py, C.c_int32), _ptr(bi, C.c_double),
                                    _ptr(bc, C.c_double), _ptr(wr, C.c_int32))
         return bi, bc, wr
+
+    def plane_edge_distance(self, vs: ViewSet, cfg: Config, best_k, px, py, inv, normals):
+        """Per hypothesis, the smallest distance (texels) from a sample of
+        its averaged views' windows to a source texel edge."""
+        px = np.ascontiguousarray(px, np.int32)
+        py = np.ascontiguousarray(py, np.int32)
+        inv = np.ascontiguousarray(inv, np.float64)
+        nrm = np.ascontiguousarray(normals, np.float64).reshape(-1, 3)
+        out = np.zeros(len(px), np.float64)
+        self.lib.orc_plane_edge_distance(C.byref(vs.struct), C.byref(cfg), best_k, len(px), _ptr(px, C.c_int32),
+                                         _ptr(py, C.c_int32), _ptr(inv, C.c_double), _ptr(nrm, C.c_double),
+                                         _ptr(out, C.c_double))
+        return out
 
     def plane_costs(self, vs: ViewSet, cfg: Config, best_k, px, py, inv, normals, half_pixel=0):
         px = np.ascontiguousarray(px, np.int32)

@@ -19,8 +19,14 @@
 //   dc / ds_k = NCC s~_k / S_ss - r~_k / sqrt(S_rr S_ss)
 // and ds_k/dp = grad I . dY/dp, so each view needs a second pass over its
 // window (the window is recomputed, never stored) accumulating, per
-// parameter vector d_k = ds_k/dp:  sum d, sum d d^T, sum s~ d, sum r~ d.  Then
+// parameter vector d_k = ds_k/dp:  sum d, sum d d^T, sum s~ d and the
+// residual sum sum e d with e_k = rho s~_k - r~_k, rho = NCC sqrt(S_rr / S_ss).
+// Then
 //   grad c = (NCC / S_ss) sum s~ d - sum r~ d / sqrt(S_rr S_ss)
+//          = sum e d / sqrt(S_rr S_ss)
+// -- the second form is what is computed: near a good match the two terms of
+// the first nearly cancel (their FP32 rounding would swamp the gradient),
+// while e_k is small per sample and its sum has no such cancellation.
 // and the Gauss-Newton matrix of the equivalent residual form
 // c = 1/2 sum_k (s^_k - r^_k)^2 (unit-normalised centred windows) is
 //   H = [sum d d^T - n m m^T - (sum s~ d)(sum s~ d)^T / S_ss] / S_ss,  m = sum d / n.
@@ -236,10 +242,12 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
                              float g[3], float H[6], float* gp, float* Hp) {
   const float* A = geo.A;
   const int hw = J.patch_half;
-  float Sd[3] = {0, 0, 0}, Sdd[6] = {0, 0, 0, 0, 0, 0}, Ssd[3] = {0, 0, 0}, Srd[3] = {0, 0, 0};
-  float Pd[6], Pdd[kPoseH], Psd[6], Prd[6];
+  float Sd[3] = {0, 0, 0}, Sdd[6] = {0, 0, 0, 0, 0, 0}, Ssd[3] = {0, 0, 0}, Sed[3] = {0, 0, 0};
+  float Pd[6], Pdd[kPoseH], Psd[6], Ped[6];
+  // residual weight: NCC sqrt(S_rr / S_ss)
+  const float rho = mo.ncc * sqrtf(mo.srr / mo.sss);
   if (kPose) {
-    for (int i = 0; i < 6; ++i) Pd[i] = Psd[i] = Prd[i] = 0.f;
+    for (int i = 0; i < 6; ++i) Pd[i] = Psd[i] = Ped[i] = 0.f;
     for (int i = 0; i < kPoseH; ++i) Pdd[i] = 0.f;
   }
   for (int dy = -hw; dy <= hw; ++dy) {
@@ -247,6 +255,7 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
       float X[3], Y[3], G[3], s, r, m, q[2];
       if (!adj_sample<kMode, true>(J, S, geo, h, dx, dy, &s, &r, X, Y, G, &m, q)) continue;
       const float st = s - mo.ms, rt = r - mo.mr;
+      const float e = fmaf(rho, st, -rt);
       // w = A^T G = dI/dX
       float w[3];
 #pragma unroll
@@ -267,7 +276,7 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
       for (int i = 0; i < 3; ++i) {
         Sd[i] += dk[i];
         Ssd[i] = fmaf(st, dk[i], Ssd[i]);
-        Srd[i] = fmaf(rt, dk[i], Srd[i]);
+        Sed[i] = fmaf(e, dk[i], Sed[i]);
 #pragma unroll
         for (int j = i; j < 3; ++j, ++t) Sdd[t] = fmaf(dk[i], dk[j], Sdd[t]);
       }
@@ -280,7 +289,7 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
         for (int i = 0; i < 6; ++i) {
           Pd[i] += pk[i];
           Psd[i] = fmaf(st, pk[i], Psd[i]);
-          Prd[i] = fmaf(rt, pk[i], Prd[i]);
+          Ped[i] = fmaf(e, pk[i], Ped[i]);
 #pragma unroll
           for (int j = i; j < 6; ++j, ++u) Pdd[u] = fmaf(pk[i], pk[j], Pdd[u]);
         }
@@ -289,18 +298,17 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
   }
   const float inv_ss = 1.0f / mo.sss;
   const float inv_rs = rsqrtf(mo.srr * mo.sss);
-  const float a = mo.ncc * inv_ss;
   const float inv_n = 1.0f / mo.n;
   int t = 0;
   for (int i = 0; i < 3; ++i) {
-    g[i] = a * Ssd[i] - inv_rs * Srd[i];
+    g[i] = inv_rs * Sed[i];
     for (int j = i; j < 3; ++j, ++t)
       H[t] = inv_ss * (Sdd[t] - Sd[i] * Sd[j] * inv_n - Ssd[i] * Ssd[j] * inv_ss);
   }
   if (kPose) {
     int u = 0;
     for (int i = 0; i < 6; ++i) {
-      gp[i] = a * Psd[i] - inv_rs * Prd[i];
+      gp[i] = inv_rs * Ped[i];
       for (int j = i; j < 6; ++j, ++u)
         Hp[u] = inv_ss * (Pdd[u] - Pd[i] * Pd[j] * inv_n - Psd[i] * Psd[j] * inv_ss);
     }
