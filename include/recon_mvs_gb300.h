@@ -420,6 +420,40 @@ RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray
                                            const recon_camera_intrinsics* intr, int32_t num_keyframes,
                                            const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
                                            recon_mvs_point_cloud* out_cloud, int32_t* out_maps);
+/* A fused point cloud left in device memory for the stage that consumes it
+ * on the GPU (UnifiedPointCloud and its Poisson input,
+ * orchestrator.cpp:1054-1064 and :181-193), so the cloud does not round-trip
+ * through host memory.  Every array is device memory on `device`, owned by the
+ * library, valid until recon_mvs_device_cloud_free; one record per voxel, in
+ * the order recon_mvs_stage_run returns them. */
+typedef struct recon_mvs_device_cloud {
+  int64_t count;
+  double* positions;   /* count x 3 */
+  double* normals;     /* count x 3, unit */
+  float* colors;       /* count x 3, zero (FuseDepthMaps writes no colour) */
+  float* confidences;  /* count */
+  float* weights;      /* count: Poisson point weights max(0, confidence) (ToOrientedCloud) */
+  int64_t* keys;       /* count: voxel keys */
+  uint32_t* counts;    /* count: points fused into each voxel */
+  double bounds_lo[3]; /* PointCloudBounds of the positions without padding (orchestrator.cpp:80-99); */
+  double bounds_hi[3]; /* +1e30 / -1e30 for an empty cloud */
+  int32_t device;      /* CUDA device ordinal of the arrays */
+  void* impl;
+} recon_mvs_device_cloud;
+
+/* recon_mvs_stage_run with the fused cloud kept in device memory (plus its
+ * Poisson weights and bounds, computed on the device).  No counterpart in the
+ * reference, whose cloud is a host vector. */
+RECON_API recon_status recon_mvs_stage_run_device(void* ctx, const uint8_t* const* gray, const int32_t* width,
+                                                  const int32_t* height, const recon_pose* poses,
+                                                  const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                                                  const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
+                                                  recon_mvs_device_cloud* out_cloud, int32_t* out_maps);
+/* Copy a device cloud into a host cloud (recon_mvs_point_cloud_free);
+ * synchronises.  `ctx` must be a context on the cloud's device. */
+RECON_API recon_status recon_mvs_device_cloud_download(void* ctx, const recon_mvs_device_cloud* cloud,
+                                                       recon_mvs_point_cloud* out);
+RECON_API void recon_mvs_device_cloud_free(recon_mvs_device_cloud* cloud);
 /* Copy a finished job's map to the host (synchronises). */
 RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out,
                                               uint32_t* out_filled);

@@ -1971,13 +1971,23 @@ static FuseMap fuse_map(int w, int h, const float* depth, const uint8_t* support
   return M;
 }
 
+// A fused cloud in device memory: one record per voxel, in the order of the
+// voxels' first points.
+struct DevCloud {
+  unsigned int n = 0;
+  DevArray<unsigned long long> key;
+  DevArray<double> pos, nrm;
+  DevArray<float> conf;
+  DevArray<unsigned int> cnt;
+};
+
 // FuseDepthMaps on device-resident maps (FuseMap: device pointers, camera):
 // the reference's voxel keys in FP64, a hash table of first occurrences,
 // buckets of points per voxel in the reference's insertion order, sequential
-// FP64 sums.  The cloud is malloc-allocated (recon_mvs_point_cloud_free).
-static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_mvs_config& cfg,
-                      recon_mvs_point_cloud* out) {
-  std::memset(out, 0, sizeof(*out));
+// FP64 sums.  The cloud stays in device memory (`out`).
+static void fuse_maps_device(Context& C, const std::vector<FuseMap>& maps, const recon_mvs_config& cfg,
+                             DevCloud* out) {
+  out->n = 0;
   if (maps.empty() || cfg.fusion_voxel_size_m <= 0.0) return;
   int64_t total = 0;
   std::vector<int64_t> base(maps.size());
@@ -2003,6 +2013,7 @@ static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_
   err.alloc(1);
   uint64_t cap = 1024;
   while (cap < 2 * (uint64_t)total) cap <<= 1;
+  if (cap > (1ull << 30)) fail(RECON_ERR_INVALID_ARGUMENT, "more pixels than one fusion call can key (2^29)");
   // cap probed slots + the side slot of the one key equal to the empty marker
   tkey.alloc(cap);
   tfirst.alloc(cap + 1);
@@ -2046,17 +2057,23 @@ static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_
   DevArray<int64_t> bucket;
   bucket.alloc(npts);
   CK(launch_fuse_scatter(total, valid.p, slot_of.p, slot_vid.p, voffset.p, cursor.p, bucket.p, C.stream));
-  DevArray<unsigned long long> okey;
-  DevArray<double> opos, onrm;
-  DevArray<float> oconf;
-  DevArray<unsigned int> ocount;
-  okey.alloc(nvox);
-  opos.alloc(3 * (size_t)nvox);
-  onrm.alloc(3 * (size_t)nvox);
-  oconf.alloc(nvox);
-  ocount.alloc(nvox);
-  CK(launch_fuse_reduce(nvox, voffset.p, vcount.p, bucket.p, key.p, pos.p, nrm.p, conf.p, okey.p, opos.p, onrm.p,
-                        oconf.p, ocount.p, C.stream));
+  out->key.alloc(nvox);
+  out->pos.alloc(3 * (size_t)nvox);
+  out->nrm.alloc(3 * (size_t)nvox);
+  out->conf.alloc(nvox);
+  out->cnt.alloc(nvox);
+  CK(launch_fuse_reduce(nvox, voffset.p, vcount.p, bucket.p, key.p, pos.p, nrm.p, conf.p, out->key.p, out->pos.p,
+                        out->nrm.p, out->conf.p, out->cnt.p, C.stream));
+  CK(cudaStreamSynchronize(C.stream));  // the working arrays are freed on return
+  out->n = nvox;
+}
+
+// The same, with the cloud copied into malloc-allocated host arrays
+// (recon_mvs_point_cloud_free).
+static void download_cloud(Context& C, const DevCloud& dc, recon_mvs_point_cloud* out) {
+  std::memset(out, 0, sizeof(*out));
+  const unsigned int nvox = dc.n;
+  if (nvox == 0) return;
   out->count = nvox;
   out->positions = (double*)std::malloc(3 * sizeof(double) * nvox);
   out->normals = (double*)std::malloc(3 * sizeof(double) * nvox);
@@ -2068,12 +2085,19 @@ static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_
     recon_mvs_point_cloud_free(out);
     fail(RECON_ERR_OUT_OF_MEMORY, "point cloud allocation failed");
   }
-  CK(cudaMemcpyAsync(out->positions, opos.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->normals, onrm.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->confidences, oconf.p, sizeof(float) * nvox, cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->keys, okey.p, sizeof(int64_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
-  CK(cudaMemcpyAsync(out->counts, ocount.p, sizeof(uint32_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->positions, dc.pos.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->normals, dc.nrm.p, 3 * sizeof(double) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->confidences, dc.conf.p, sizeof(float) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->keys, dc.key.p, sizeof(int64_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
+  CK(cudaMemcpyAsync(out->counts, dc.cnt.p, sizeof(uint32_t) * nvox, cudaMemcpyDeviceToHost, C.stream));
   CK(cudaStreamSynchronize(C.stream));
+}
+
+static void fuse_maps(Context& C, const std::vector<FuseMap>& maps, const recon_mvs_config& cfg,
+                      recon_mvs_point_cloud* out) {
+  DevCloud dc;
+  fuse_maps_device(C, maps, cfg, &dc);
+  download_cloud(C, dc, out);
 
 }
 
@@ -2266,15 +2290,18 @@ RECON_API recon_status recon_mvs_jobs_run(void* ctx, const int32_t* jobs, int32_
 // and a progress report after it; maps with nothing filled are dropped; the
 // rest are fused (optionally behind the geometric-consistency filter) on the
 // device.
-RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray, const int32_t* width,
-                                           const int32_t* height, const recon_pose* poses,
-                                           const recon_camera_intrinsics* intr, int32_t num_keyframes,
-                                           const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
-                                           recon_mvs_point_cloud* out_cloud, int32_t* out_maps) {
-  return guard([&] {
-    if (!ctx || !gray || !width || !height || !poses || !intr || !cfg || !out_cloud)
+}  // extern "C"
+
+// The stage up to its fusion: staging, source selection, batched runs,
+// consistency; then `fuse(maps)` with the produced maps (device pointers of
+// jobs that live until it returns).
+template <class Fuse>
+static void stage_core(void* ctx, const uint8_t* const* gray, const int32_t* width, const int32_t* height,
+                       const recon_pose* poses, const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                       const recon_mvs_config* cfg, const recon_mvs_stage_params* params, int32_t* out_maps,
+                       Fuse&& fuse) {
+    if (!ctx || !gray || !width || !height || !poses || !intr || !cfg)
       fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
-    std::memset(out_cloud, 0, sizeof(*out_cloud));
     if (out_maps) *out_maps = 0;
     recon_mvs_stage_params P;
     std::memset(&P, 0, sizeof(P));
@@ -2372,10 +2399,113 @@ RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray
       fm.push_back(fuse_map(D.w, D.h, D.out_depth.p, D.out_support.p, D.out_conf.p, keep[i] ? keep[i]->p : nullptr,
                             img[r]->intr, poses[r], nrm));
     }
-    fuse_maps(C, fm, *cfg, out_cloud);
+    fuse(C, fm);
     if (out_maps) *out_maps = (int32_t)produced.size();
+}
+
+extern "C" {
+
+RECON_API recon_status recon_mvs_stage_run(void* ctx, const uint8_t* const* gray, const int32_t* width,
+                                           const int32_t* height, const recon_pose* poses,
+                                           const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                                           const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
+                                           recon_mvs_point_cloud* out_cloud, int32_t* out_maps) {
+  return guard([&] {
+    if (!out_cloud) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out_cloud, 0, sizeof(*out_cloud));
+    stage_core(ctx, gray, width, height, poses, intr, num_keyframes, cfg, params, out_maps,
+               [&](Context& C, const std::vector<FuseMap>& fm) { fuse_maps(C, fm, *cfg, out_cloud); });
   });
 }
+
+// ---------------------------------------------------------------------------
+// device-resident clouds
+// ---------------------------------------------------------------------------
+struct DeviceCloudImpl {
+  int device = 0;
+  DevCloud c;
+  DevArray<float> colors, weights;
+};
+
+static void free_device_cloud(recon_mvs_device_cloud* out) {
+  if (!out) return;
+  auto* impl = static_cast<DeviceCloudImpl*>(out->impl);
+  if (impl) {
+    cudaSetDevice(impl->device);  // the arrays belong to that device
+    delete impl;
+  }
+  std::memset(out, 0, sizeof(*out));
+}
+
+// Fills `out` from a device fusion result: the voxel records, zero colours
+// (FuseDepthMaps writes none), the Poisson point weights max(0, confidence)
+// (UnifiedPointCloud::ToOrientedCloud, orchestrator.cpp:181-193) and the
+// bounds of the positions (PointCloudBounds without padding,
+// orchestrator.cpp:80-99).
+static void publish_device_cloud(Context& C, std::unique_ptr<DeviceCloudImpl> impl, recon_mvs_device_cloud* out) {
+  const unsigned int n = impl->c.n;
+  double bounds[6] = {1e30, 1e30, 1e30, -1e30, -1e30, -1e30};
+  if (n > 0) {
+    impl->colors.alloc(3 * (size_t)n);
+    impl->weights.alloc(n);
+    CK(cudaMemsetAsync(impl->colors.p, 0, 3 * sizeof(float) * (size_t)n, C.stream));
+    DevArray<double> b;
+    b.alloc(6);
+    CK(launch_cloud_finish(impl->c.pos.p, impl->c.conf.p, n, impl->weights.p, b.p, C.stream));
+    CK(cudaMemcpyAsync(bounds, b.p, sizeof(bounds), cudaMemcpyDeviceToHost, C.stream));
+    CK(cudaStreamSynchronize(C.stream));
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->count = n;
+  out->positions = impl->c.pos.p;
+  out->normals = impl->c.nrm.p;
+  out->colors = impl->colors.p;
+  out->confidences = impl->c.conf.p;
+  out->weights = impl->weights.p;
+  out->keys = reinterpret_cast<int64_t*>(impl->c.key.p);
+  out->counts = impl->c.cnt.p;
+  for (int i = 0; i < 3; ++i) {
+    out->bounds_lo[i] = bounds[i];
+    out->bounds_hi[i] = bounds[3 + i];
+  }
+  out->device = C.device;
+  impl->device = C.device;
+  out->impl = impl.release();
+}
+
+RECON_API recon_status recon_mvs_stage_run_device(void* ctx, const uint8_t* const* gray, const int32_t* width,
+                                                  const int32_t* height, const recon_pose* poses,
+                                                  const recon_camera_intrinsics* intr, int32_t num_keyframes,
+                                                  const recon_mvs_config* cfg, const recon_mvs_stage_params* params,
+                                                  recon_mvs_device_cloud* out_cloud, int32_t* out_maps) {
+  return guard([&] {
+    if (!out_cloud) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out_cloud, 0, sizeof(*out_cloud));
+    stage_core(ctx, gray, width, height, poses, intr, num_keyframes, cfg, params, out_maps,
+               [&](Context& C, const std::vector<FuseMap>& fm) {
+                 auto impl = std::make_unique<DeviceCloudImpl>();
+                 fuse_maps_device(C, fm, *cfg, &impl->c);
+                 publish_device_cloud(C, std::move(impl), out_cloud);
+               });
+  });
+}
+
+RECON_API recon_status recon_mvs_device_cloud_download(void* ctx, const recon_mvs_device_cloud* cloud,
+                                                       recon_mvs_point_cloud* out) {
+  return guard([&] {
+    if (!ctx || !cloud || !out) fail(RECON_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    const auto* impl = static_cast<const DeviceCloudImpl*>(cloud->impl);
+    if (!impl && cloud->count > 0) fail(RECON_ERR_INVALID_ARGUMENT, "not a library device cloud");
+    if (!impl) return;
+    Context& C = *static_cast<Context*>(ctx);
+    if (impl->device != C.device) fail(RECON_ERR_INVALID_ARGUMENT, "the cloud lives on another device");
+    C.use();
+    download_cloud(C, impl->c, out);
+  });
+}
+
+RECON_API void recon_mvs_device_cloud_free(recon_mvs_device_cloud* cloud) { free_device_cloud(cloud); }
 
 RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out, uint32_t* filled) {
   return guard([&] {

@@ -436,6 +436,49 @@ cudaError_t launch_fuse_reduce(unsigned int nvox, const unsigned int* voffset, c
   return cudaGetLastError();
 }
 
+// A fused cloud's Poisson point weights max(0, confidence) and the bounds of
+// its positions (min x, y, z, max x, y, z), one block: the order of the
+// min / max reduction does not change its result.
+constexpr int kBoundsThreads = 512;
+__global__ void __launch_bounds__(kBoundsThreads) k_cloud_finish(const double* __restrict__ pos,
+                                                                 const float* __restrict__ conf, unsigned int n,
+                                                                 float* weights, double* bounds) {
+  __shared__ double red[6][kBoundsThreads];
+  double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
+  for (unsigned int i = threadIdx.x; i < n; i += kBoundsThreads) {
+    weights[i] = fmaxf(0.0f, conf[i]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double v = pos[3 * (size_t)i + q];
+      lo[q] = fmin(lo[q], v);
+      hi[q] = fmax(hi[q], v);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    red[q][threadIdx.x] = lo[q];
+    red[3 + q][threadIdx.x] = hi[q];
+  }
+  __syncthreads();
+  for (int off = kBoundsThreads / 2; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        red[q][threadIdx.x] = fmin(red[q][threadIdx.x], red[q][threadIdx.x + off]);
+        red[3 + q][threadIdx.x] = fmax(red[3 + q][threadIdx.x], red[3 + q][threadIdx.x + off]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) bounds[threadIdx.x] = red[threadIdx.x][0];
+}
+
+cudaError_t launch_cloud_finish(const double* pos, const float* conf, unsigned int n, float* weights, double* bounds,
+                                cudaStream_t st) {
+  k_cloud_finish<<<1, kBoundsThreads, 0, st>>>(pos, conf, n, weights, bounds);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_consistency(const ConsistencyRef& R, const ConsistencySrc* S, int num_src, float rel_max,
                                float reproj_px_max, int min_views, uint8_t* count, uint8_t* keep, cudaStream_t st) {
   const dim3 b(32, 8);

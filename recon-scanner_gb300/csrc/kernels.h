@@ -114,7 +114,7 @@ struct PlaneBatch {
   int start[kBatchJobs + 1];
   int njobs;
   // sweeps: one TMA tensor map per job over its ref_de planes (device memory,
-  // 64-byte aligned), box = 48 columns x (rows + 2H) rows x 2 planes
+  // 64-byte aligned), box = kTileCols columns x (rows + 2H) rows x 2 planes
   const CUtensorMap* tmaps;
   int* err;  // set when a TMA wait runs out (the launch then stops early)
 };
@@ -163,6 +163,8 @@ cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const u
                                int* samples, cudaStream_t st);
 
 // ---- fusion ----
+cudaError_t launch_cloud_finish(const double* pos, const float* conf, unsigned int n, float* weights, double* bounds,
+                                cudaStream_t st);
 cudaError_t launch_fuse_points(const FuseMap& M, int64_t base, const FuseParams& P, unsigned long long* key,
                                double* pos, double* nrm, float* conf, uint8_t* valid, cudaStream_t st);
 cudaError_t launch_fuse_insert(int64_t n, const unsigned long long* key, const uint8_t* valid,

@@ -119,6 +119,13 @@ class PointCloudC(C.Structure):
                 ("keys", C.POINTER(C.c_int64)), ("counts", C.POINTER(C.c_uint32))]
 
 
+class DeviceCloudC(C.Structure):
+    _fields_ = [("count", C.c_int64), ("positions", C.c_void_p), ("normals", C.c_void_p), ("colors", C.c_void_p),
+                ("confidences", C.c_void_p), ("weights", C.c_void_p), ("keys", C.c_void_p), ("counts", C.c_void_p),
+                ("bounds_lo", C.c_double * 3), ("bounds_hi", C.c_double * 3), ("device", C.c_int32),
+                ("impl", C.c_void_p)]
+
+
 class Stats(C.Structure):
     _fields_ = [("hypotheses_evaluated", C.c_uint64), ("last_run_ms", C.c_double), ("last_sweep_ms", C.c_double),
                 ("last_sweep_launches", C.c_int32), ("tile_rows", C.c_int32), ("ctas_per_sm", C.c_int32),
@@ -201,6 +208,12 @@ _SIGS = {
                                       C.POINTER(C.c_int32), C.POINTER(Pose), C.POINTER(Intrinsics), C.c_int32,
                                       C.POINTER(MvsConfig), C.POINTER(StageParams), C.POINTER(PointCloudC),
                                       C.POINTER(C.c_int32)]),
+    "recon_mvs_stage_run_device": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_int32), C.POINTER(Pose), C.POINTER(Intrinsics), C.c_int32,
+                                             C.POINTER(MvsConfig), C.POINTER(StageParams), C.POINTER(DeviceCloudC),
+                                             C.POINTER(C.c_int32)]),
+    "recon_mvs_device_cloud_download": (C.c_int, [C.c_void_p, C.POINTER(DeviceCloudC), C.POINTER(PointCloudC)]),
+    "recon_mvs_device_cloud_free": (None, [C.POINTER(DeviceCloudC)]),
     "recon_mvs_job_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -347,6 +360,57 @@ class PointCloud:
 
     def size(self):
         return len(self.positions)
+
+
+class _DeviceArray:
+    """A device array of a DeviceCloud seen through __cuda_array_interface__
+    (torch.as_tensor(view, device="cuda") wraps it without a copy)."""
+
+    def __init__(self, ptr, shape, typestr, owner):
+        self._owner = owner  # keeps the cloud alive while the view is used
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (int(ptr or 0), False),
+                                         "version": 3}
+
+
+class DeviceCloud:
+    """A fused cloud left in device memory (recon_mvs_device_cloud): one
+    record per voxel; .array(name) views a field on the device, .download()
+    copies the cloud to the host, .free() releases it."""
+
+    _FIELDS = {"positions": (3, "<f8"), "normals": (3, "<f8"), "colors": (3, "<f4"), "confidences": (1, "<f4"),
+               "weights": (1, "<f4"), "keys": (1, "<i8"), "counts": (1, "<u4")}
+
+    def __init__(self, engine, c: DeviceCloudC):
+        self.engine = engine
+        self.c = c
+
+    @property
+    def count(self):
+        return int(self.c.count)
+
+    @property
+    def bounds(self):
+        return np.array(list(self.c.bounds_lo)), np.array(list(self.c.bounds_hi))
+
+    def array(self, name):
+        k, t = self._FIELDS[name]
+        shape = (self.count, k) if k > 1 else (self.count,)
+        return _DeviceArray(getattr(self.c, name), shape, t, self)
+
+    def download(self) -> "PointCloud":
+        pc = PointCloudC()
+        _check(_lib().recon_mvs_device_cloud_download(self.engine.ctx, C.byref(self.c), C.byref(pc)))
+        return _take_cloud(pc)
+
+    def free(self):
+        if self.c.impl:
+            _lib().recon_mvs_device_cloud_free(C.byref(self.c))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:  # noqa: BLE001 -- interpreter shutdown
+            pass
 
 
 # ----------------------------------------------------------------------------
@@ -625,6 +689,27 @@ class Engine:
                                           C.cast(ks, C.POINTER(Intrinsics)), n, C.byref(config), C.byref(prm),
                                           C.byref(pc), C.byref(maps)))
         return _take_cloud(pc), maps.value
+
+    def stage_run_device(self, images, poses, intrinsics_list, config: MvsConfig, undistort=False, batch_size=0,
+                         consistency_views=0, rel_depth=0.01, reproj_px=1.0, plane_normals=False):
+        """stage_run with the fused cloud kept in device memory -> (DeviceCloud,
+        maps fused)."""
+        n = len(images)
+        imgs = [None if im is None else np.ascontiguousarray(im, np.uint8) for im in images]
+        ptrs = (C.POINTER(C.c_uint8) * max(1, n))(*[None if im is None else _ptr(im, C.c_uint8) for im in imgs])
+        w = np.asarray([0 if im is None else im.shape[1] for im in imgs] or [0], np.int32)
+        h = np.asarray([0 if im is None else im.shape[0] for im in imgs] or [0], np.int32)
+        ps = (Pose * max(1, n))(*[pose(p) for p in poses])
+        ks = (Intrinsics * max(1, n))(*[intrinsics(k) for k in intrinsics_list])
+        prm = StageParams(int(undistort), int(batch_size), int(consistency_views), int(plane_normals), rel_depth,
+                          reproj_px, CANCEL_FN(0), PROGRESS_FN(0), None)
+        dc = DeviceCloudC()
+        maps = C.c_int32()
+        _check(_lib().recon_mvs_stage_run_device(self.ctx, C.cast(ptrs, C.POINTER(C.POINTER(C.c_uint8))),
+                                                 _ptr(w, C.c_int32), _ptr(h, C.c_int32), C.cast(ps, C.POINTER(Pose)),
+                                                 C.cast(ks, C.POINTER(Intrinsics)), n, C.byref(config), C.byref(prm),
+                                                 C.byref(dc), C.byref(maps)))
+        return DeviceCloud(self, dc), maps.value
 
     def release(self, job: int):
         _check(_lib().recon_mvs_job_release(self.ctx, job))

@@ -163,3 +163,42 @@ def test_bgra_frames(mvs, orc, capture):
         eng.close()
     np.testing.assert_array_equal(maps[0].depth, maps[1].depth)
     np.testing.assert_array_equal(maps[0].cost, maps[1].cost)
+
+
+def test_stage_run_device_cloud(mvs, capture):
+    """recon_mvs_stage_run_device keeps the fused cloud in device memory for
+    the next stage on the GPU: downloaded, it equals recon_mvs_stage_run's
+    cloud bit for bit; its Poisson weights are max(0, confidence)
+    (UnifiedPointCloud::ToOrientedCloud), its colours zero and its bounds the
+    positions' min / max (PointCloudBounds); torch reads its arrays in place."""
+    import torch
+
+    cams = [v.camera for v in capture.views]
+    imgs = [v.image for v in capture.views]
+    poses = [c.pose_array() for c in cams]
+    intr = [c.intrinsics_array() for c in cams]
+    cfg = cfg_of(mvs, capture)
+    eng = mvs.Engine(mvs.Options(mode=mvs.MODE_PLANE, best_k=3, device=0))
+    try:
+        want, n_want = eng.stage_run(imgs, poses, intr, cfg, consistency_views=2, plane_normals=True)
+        dc, n_got = eng.stage_run_device(imgs, poses, intr, cfg, consistency_views=2, plane_normals=True)
+        assert n_got == n_want and dc.count == want.size() > 1000 and dc.c.device == 0
+        got = dc.download()
+        for name in ("positions", "normals", "confidences", "keys", "counts", "colors"):
+            np.testing.assert_array_equal(getattr(got, name), getattr(want, name), err_msg=name)
+        pos = torch.as_tensor(dc.array("positions"), device="cuda")
+        conf = torch.as_tensor(dc.array("confidences"), device="cuda")
+        w = torch.as_tensor(dc.array("weights"), device="cuda")
+        col = torch.as_tensor(dc.array("colors"), device="cuda")
+        assert pos.shape == (dc.count, 3) and pos.dtype == torch.float64
+        np.testing.assert_array_equal(pos.cpu().numpy(), want.positions)
+        np.testing.assert_array_equal(w.cpu().numpy(), np.maximum(0.0, want.confidences))
+        assert torch.equal(w, torch.clamp(conf, min=0.0))
+        assert int(torch.count_nonzero(col)) == 0
+        lo, hi = dc.bounds
+        np.testing.assert_array_equal(lo, want.positions.min(0))
+        np.testing.assert_array_equal(hi, want.positions.max(0))
+        dc.free()
+        assert dc.c.impl is None and dc.count == 0
+    finally:
+        eng.close()
