@@ -13,10 +13,15 @@ staged; the capture's consistency + fusion stage is reported beside it.
             persistent launch per half-sweep, replayed from a CUDA graph),
             source images stored as FP16 textures, window samples
             interpolated by the texture unit, Gauss-Newton refinement from
-            the adjoint; the plain path (FP32 textures, exact FP32
+            the adjoint, coarse-to-fine initialisation (iterations 1-2 of the
+            8 on the half-resolution pyramid level, as the reference design
+            lays out its search: level 1 for the coarse rounds, level 0 for
+            the fine ones); the plain path (FP32 textures, exact FP32
             interpolation, one launch per view, the reference's
-            golden-section refinement) is timed in the same run and reported
-            under "plain" with its depth agreement;
+            golden-section refinement, all 8 iterations at full resolution)
+            is timed in the same run and reported under "plain" with its
+            depth agreement, and the forms between the two under
+            "attribution";
   value  -- depth maps/s with the staged inputs resident in HBM; each step
             is timed with CUDA events on the engine's stream and L2 is
             flushed (a 512 MiB write) between steps, outside the events;
@@ -567,18 +572,19 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
 
     import synthetic as Syn
 
-    forms = [("batched_fp32_exact_golden", False, 0, 1), ("batched_fp16_exact_golden", True, 0, 1),
-             ("batched_fp16_exact_gauss_newton", True, 0, 2)]
+    forms = [("batched_fp32_exact_golden", False, 0, 1, 0), ("batched_fp16_exact_golden", True, 0, 1, 0),
+             ("batched_fp16_exact_gauss_newton", True, 0, 2, 0),
+             ("batched_fp16_texture_gauss_newton_full_resolution", True, 1, 2, 0)]
     out = {"steps": args.attr_steps, "forms": {}}
-    for name, fp16, interp, refine in forms:
-        ms, _, _, _, fmaps, _ = time_form(M, views, cfgs, mk(fp16, interp, False, refine), args.attr_steps, 1,
+    for name, fp16, interp, refine, coarse in forms:
+        ms, _, _, _, fmaps, _ = time_form(M, views, cfgs, mk(fp16, interp, False, refine, coarse), args.attr_steps, 1,
                                           flush, world, undistort, scenes=scenes)
         tot = barrier_max(world, float(sum(ms)))
         med, p95 = agreement(fmaps, chosen_maps)
         out["forms"][name] = {"value": world * len(views) * args.attr_steps / (tot / 1000.0),
                               "accuracy": accuracy(fmaps, truths, rng),
                               "vs_chosen_median_rel_depth_diff": med, "vs_chosen_p95_rel_depth_diff": p95}
-    out["forms"]["chosen_fp16_texture_gauss_newton"] = {"value": chosen_value}
+    out["forms"]["chosen"] = {"value": chosen_value, "form": "the timed form of this line"}
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -610,8 +616,10 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
                       "p99_abs": float(np.quantile(d, 0.99)), "max_abs": float(d.max()),
                       "within_1e-5_rel_plus_2e-6": float(np.mean(d <= 1e-5 * np.abs(want[ok]) + 2e-6))}
     out["cost_vs_fp64_oracle"] = cost
-    out["note"] = ("plain = FP32 storage, exact interpolation, one launch per view, golden section; each form adds "
-                   "one change; chosen = batched, FP16, Gauss-Newton, texture-unit interpolation (8-bit weights)")
+    out["note"] = ("plain = FP32 storage, exact interpolation, one launch per view, golden section, every iteration "
+                   "at full resolution; each form adds one change: batched, FP16 storage, Gauss-Newton, texture-unit "
+                   "interpolation (8-bit weights); chosen adds coarse-to-fine (the first iterations on the "
+                   "half-resolution level, the same total)")
     return out
 
 
@@ -751,10 +759,10 @@ def run_gpu(args):
     s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
     # FLOP model: per source window sampled K*K*26 + 30, per hypothesis 40
     flop_per_window, flop_per_hyp_setup = K * K * 26 + 30, 40
-    mk = lambda fp16, interp, per_view, refine: M.Options(
+    mk = lambda fp16, interp, per_view, refine, coarse=args.coarse: M.Options(
         mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
         refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
-        tile_rows=args.tile_rows)
+        tile_rows=args.tile_rows, coarse_iterations=coarse)
     opts = mk(args.fp16, args.interp, args.per_view, args.refine)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -771,7 +779,7 @@ def run_gpu(args):
     if not args.plain and not args.chosen_only:
         p_fp16 = False if WORKLOAD != "c3" else args.fp16
         p_interp = 0 if WORKLOAD != "c3" else args.interp
-        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True, 1), args.steps,
+        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True, 1, 0), args.steps,
                                                       args.warmup, flush, world, undistort, scenes=scenes)
         p_total = barrier_max(world, float(sum(p_ms)))
         med, p95 = agreement(maps, p_maps)
@@ -844,7 +852,9 @@ def run_gpu(args):
 
     form = (f"{'fp16' if args.fp16 else 'fp32'} storage, {'texture-unit' if args.interp else 'exact fp32'} "
             f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
-            f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}")
+            f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}"
+            + (f", coarse-to-fine: iterations 1-{args.coarse} of {ITERS} on the half-resolution level (2x2 means)"
+               if args.coarse else ", every iteration at full resolution"))
     wl = describe_workload(scenes)
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -852,7 +862,8 @@ def run_gpu(args):
             "data": "synthetic (seeded scenes, analytic truth)",
             "config": {"workload": f"{wl}; {K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}",
                        "maps_per_step": n_maps, "megapixels_per_step": sum(pixels) / 1e6,
-                       "form": form, "tile_rows": st.tile_rows, "ctas_per_sm": st.ctas_per_sm,
+                       "form": form, "coarse_iterations": args.coarse, "tile_rows": st.tile_rows,
+                       "ctas_per_sm": st.ctas_per_sm,
                        "prefilter": bool(args.prefilter), "sampling": args.sampling,
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}"},
@@ -1205,6 +1216,9 @@ def main():
     ap.add_argument("--per-view", action="store_true", help="one launch per view instead of the batched form")
     ap.add_argument("--tile-rows", type=int, default=0, help="sweep tile rows (2, 4, 8); 0 = autotuned")
     ap.add_argument("--depth-range", default=None, help="the tabletop capture's search range 'lo,hi' in metres")
+    ap.add_argument("--coarse", type=int, default=None,
+                    help="coarse-to-fine: the first N of the iterations on the half-resolution level (chosen form "
+                         "default 2, the reference design's rounds 1-2 on pyramid level 1; 0 = off)")
     args = ap.parse_args()
     set_workload(args.workload)
     if args.depth_range:
@@ -1214,6 +1228,8 @@ def main():
     # the plain FP32 path is timed beside it unless --plain asks for it alone
     if args.refine is None:
         args.refine = 1 if (args.plain or args.workload == "c3") else 2
+    if args.coarse is None:
+        args.coarse = 0 if (args.plain or args.workload == "c3") else 2
     if args.plain:
         args.fp16, args.interp, args.per_view = False, 0, True
     elif args.workload == "c3":

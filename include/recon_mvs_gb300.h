@@ -159,7 +159,11 @@ typedef struct recon_mvs_options {
                          a propagation candidate equal to the one just rejected, and the remaining
                          windows of a candidate once its best-k bound shows it cannot be taken (the
                          maps are the same; a switch for checks and timing) */
-  int32_t reserved[1];
+  int32_t coarse_iterations; /* plane mode: 0 = off; n > 0 (and n < the configured iterations) = the
+                                first n iterations run on a half-resolution pyramid level (2x2 means of
+                                the staged images, focal lengths and principal point halved), and the
+                                full-resolution search starts from the planes they found: coarse-to-fine
+                                initialisation, the configured iteration count in total */
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list

@@ -218,6 +218,14 @@ struct Job {
   float* out_normal;        // optional
   float* out_cost;          // optional
   unsigned int* out_filled; // zeroed by the init kernel, counted by the output kernel
+  // coarse-to-fine initialisation (optional): the plane state of this view's
+  // half-resolution search; pixel (x, y) starts from the plane of its parent
+  // (x / 2, y / 2), carried to its own ray
+  const float4* coarse_hyp;
+  const float* coarse_cost;
+  int coarse_w, coarse_h;
+  float crfx, crfy, crcx, crcy;  // the half-resolution reference intrinsics
+  int iter_offset;               // iterations run at the coarse level: the schedule continues from there
 };
 
 // Per-pixel ray of the reference camera, FP64: pinhole fast path, or the

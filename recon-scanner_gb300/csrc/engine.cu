@@ -186,6 +186,7 @@ struct StagedImage {
   DevArray<float> ref, box, de;
   int de_pitch = 0;  // floats per row of `de` (a multiple of 4: 16-byte rows for TMA)
   bool has_ref = false;
+  std::shared_ptr<StagedImage> half;  // pyramid level 1, made on first use
   const void* dev() const { return is_f32 ? (const void*)f32.p : (const void*)u8.p; }
 };
 
@@ -216,6 +217,7 @@ struct JobData {
   recon_pose ref_pose{};
   recon_camera_intrinsics ref_intr{};  // as matched (pinhole after undistortion)
   std::vector<recon_pose> src_pose;    // per relative source k
+  std::unique_ptr<JobData> coarse;     // the half-resolution search of coarse-to-fine initialisation
 };
 
 // ---- plane-mode batch plans (used by the context below) ----
@@ -270,6 +272,7 @@ struct PlanePlan {
   std::vector<int> ids;
   bool per_view = false;
   std::vector<std::unique_ptr<PlaneGroup>> groups;
+  std::vector<std::unique_ptr<PlaneGroup>> coarse_groups;  // half-resolution searches, run in the init stage
   cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // init, sweeps, refine + output
   int sweep_launches = 0;
   ~PlanePlan() {
@@ -582,11 +585,62 @@ static void ensure_reference(Context& C, StagedImage& I) {
   I.has_ref = true;
 }
 
+// Pyramid level 1 of a staged image (kept with it: a capture's views are
+// reduced once): 2 x 2 means, intrinsics of the half-resolution camera.
+static std::shared_ptr<StagedImage> half_level(Context& C, const std::shared_ptr<StagedImage>& I) {
+  if (I->half) return I->half;
+  auto L = std::make_shared<StagedImage>();
+  L->w = I->w / 2;
+  L->h = I->h / 2;
+  L->intr = I->intr;
+  L->intr.fx *= 0.5;
+  L->intr.fy *= 0.5;
+  L->intr.cx *= 0.5;
+  L->intr.cy *= 0.5;
+  L->intr.width = L->w;
+  L->intr.height = L->h;
+  L->is_f32 = true;
+  L->f32.alloc((size_t)L->w * L->h);
+  CK(launch_half_level(I->is_f32 ? nullptr : I->u8.p, I->is_f32 ? I->f32.p : nullptr, I->w, I->h, L->f32.p,
+                       C.stream));
+  I->half = L;
+  return L;
+}
+
+// Coarse-to-fine initialisation applies to a plane-mode job when it asks for
+// fewer coarse iterations than its configuration runs and the half-resolution
+// level still holds a few windows.
+static int coarse_iterations(const Context& C, const recon_mvs_config& cfg, int w, int h) {
+  const int n = C.opts.coarse_iterations;
+  if (C.opts.mode != RECON_MVS_MODE_PLANE || n <= 0 || n >= cfg.iterations) return 0;
+  const int min_side = 4 * (cfg.patch_size | 1);
+  return (w / 2 >= min_side && h / 2 >= min_side) ? n : 0;
+}
+
+static std::unique_ptr<JobData> build_job_data(Context& C, const std::shared_ptr<StagedImage>& ref,
+                                               const std::vector<std::shared_ptr<StagedImage>>& srcs,
+                                               const recon_pose& ref_pose, const std::vector<recon_pose>& src_poses,
+                                               const recon_mvs_config* cfg, const double* seeds, int num_seeds,
+                                               bool coarse_level);
+
 // A job from staged images: the reference, its sources and their poses.
 static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
                      const std::vector<std::shared_ptr<StagedImage>>& srcs, const recon_pose& ref_pose,
                      const std::vector<recon_pose>& src_poses, const recon_mvs_config* cfg, const double* seeds,
                      int num_seeds) {
+  auto jd = build_job_data(C, ref, srcs, ref_pose, src_poses, cfg, seeds, num_seeds, false);
+  const int id = C.next_id++;
+  C.jobs[id] = std::move(jd);
+  return id;
+}
+
+// `coarse_level`: the half-resolution search of another job (no seeds, no
+// refinement, no outputs read).
+static std::unique_ptr<JobData> build_job_data(Context& C, const std::shared_ptr<StagedImage>& ref,
+                                               const std::vector<std::shared_ptr<StagedImage>>& srcs,
+                                               const recon_pose& ref_pose, const std::vector<recon_pose>& src_poses,
+                                               const recon_mvs_config* cfg, const double* seeds, int num_seeds,
+                                               bool coarse_level) {
   if (!cfg) fail(RECON_ERR_INVALID_ARGUMENT, "config is NULL");
   if (cfg->patch_size < 1) fail(RECON_ERR_INVALID_ARGUMENT, "patch_size < 1");
   if (srcs.empty()) fail(RECON_ERR_INVALID_ARGUMENT, "no source views");
@@ -701,7 +755,9 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
   J.best_k = C.opts.best_k;
   J.prune = C.opts.exhaustive ? 0 : 1;
   J.seed = C.opts.seed;
-  J.eval_counter = C.counter.p;
+  // the counters measure the full-resolution sweeps (the roofline's launches);
+  // a coarse level's sweeps are not counted
+  J.eval_counter = coarse_level ? nullptr : C.counter.p;
 
   const size_t npx = (size_t)D.w * D.h;
   if (plane) {
@@ -750,8 +806,9 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
     // Gauss-Newton: one Levenberg-Marquardt step (up to four damping
     // retries) -- further steps did not lower the error at the measured
     // image noise, and each costs about one golden-section search
-    J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0) ? (C.opts.refine == 2 ? 1 : cfg->subpixel_iterations)
-                                                                     : 0;
+    J.refine_iters = (C.opts.refine && cfg->subpixel_iterations > 0 && !coarse_level)
+                         ? (C.opts.refine == 2 ? 1 : cfg->subpixel_iterations)
+                         : 0;
     J.refine_mode = C.opts.refine;
     J.inv_per_px = (float)D.inv_per_px;
     J.out_depth = D.out_depth.p;
@@ -760,11 +817,28 @@ static int build_job(Context& C, const std::shared_ptr<StagedImage>& ref,
     J.out_normal = D.out_normal.p;
     J.out_cost = D.out_cost.p;
     J.out_filled = D.filled.p;
+    const int nc = coarse_level ? 0 : coarse_iterations(C, *cfg, D.w, D.h);
+    if (nc > 0) {
+      std::vector<std::shared_ptr<StagedImage>> half_srcs;
+      for (const auto& I : srcs) half_srcs.push_back(half_level(C, I));
+      recon_mvs_config c1 = *cfg;
+      c1.iterations = nc;
+      D.coarse = build_job_data(C, half_level(C, ref), half_srcs, ref_pose, src_poses, &c1, nullptr, 0, true);
+      const JobData& L = *D.coarse;
+      J.coarse_hyp = L.hyp.p;
+      J.coarse_cost = L.cost.p;
+      J.coarse_w = L.w;
+      J.coarse_h = L.h;
+      J.crfx = L.J.rfx;
+      J.crfy = L.J.rfy;
+      J.crcx = L.J.rcx;
+      J.crcy = L.J.rcy;
+      J.iter_offset = nc;
+      J.iterations = cfg->iterations - nc;
+    }
   }
   CK(cudaStreamSynchronize(C.stream));
-  const int id = C.next_id++;
-  C.jobs[id] = std::move(jd);
-  return id;
+  return jd;
 }
 
 // The PatchMatchStereo argument list (reference index contract): every image
@@ -831,7 +905,7 @@ static void encode_ref_tile_map(const JobData& D, int box_rows, CUtensorMap* out
 
 static void build_group(Context& C, PlaneGroup& G) {
   std::stable_sort(G.jobs.begin(), G.jobs.end(), [](const JobData* a, const JobData* b) {
-    if (a->cfg.iterations != b->cfg.iterations) return a->cfg.iterations > b->cfg.iterations;
+    if (a->J.iterations != b->J.iterations) return a->J.iterations > b->J.iterations;
     return (long long)a->w * a->h > (long long)b->w * b->h;
   });
   const int n = G.nj();
@@ -850,7 +924,7 @@ static void build_group(Context& C, PlaneGroup& G) {
   for (int j = 0; j < n; ++j) {
     const JobData& D = *G.jobs[j];
     G.max_src = std::max(G.max_src, D.num_src);
-    G.max_iters = std::max(G.max_iters, std::max(0, D.cfg.iterations));
+    G.max_iters = std::max(G.max_iters, std::max(0, D.J.iterations));
     G.refine_any = G.refine_any || (D.J.refine_iters > 0 && D.J.refine_mode == 1);
     G.refine_gn = G.refine_gn || (D.J.refine_iters > 0 && D.J.refine_mode == 2);
     G.pixels += (long long)D.w * D.h;
@@ -878,7 +952,7 @@ static void build_group(Context& C, PlaneGroup& G) {
   G.active.assign(std::max(G.max_iters, 1), 0);
   for (int it = 0; it < G.max_iters; ++it)
     for (int j = 0; j < n; ++j)
-      if (G.jobs[j]->cfg.iterations > it) G.active[it] = j + 1;
+      if (G.jobs[j]->J.iterations > it) G.active[it] = j + 1;
   G.queues.alloc(std::max(2 * G.max_iters, 1));
 }
 
@@ -967,6 +1041,16 @@ static void tune_group(Context& C, PlaneGroup& G) {
 // between the graph launches and bracket the sweeps exactly.
 static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
   if (stage == 0) {
+    // coarse-to-fine: the half-resolution searches first; the full-resolution
+    // init then starts each pixel from its parent's plane
+    for (auto& g : P.coarse_groups) {
+      PlaneGroup& G = *g;
+      CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+      for (int it = 0; it < G.max_iters; ++it)
+        for (int color = 0; color < 2; ++color)
+          CK(launch_plane_sweep(G.sweep_batch(G.rows), G.sweep_total(G.rows, it), G.queues.p + 2 * it + color,
+                                G.patch_half, G.mode, G.max_src, G.rows, G.grid, color, it, C.stream));
+    }
     for (auto& g : P.groups) {
       PlaneGroup& G = *g;
       CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
@@ -1027,21 +1111,28 @@ static std::unique_ptr<PlanePlan> make_plan(Context& C, const std::vector<JobDat
   auto P = std::make_unique<PlanePlan>();
   P->ids = ids;
   P->per_view = C.opts.per_view != 0;
-  for (JobData* D : jobs) {
-    PlaneGroup* G = nullptr;
-    if (!P->per_view)
-      for (auto& g : P->groups)
-        if (g->patch_half == D->J.patch_half && g->mode == D->J.src_mode && g->nj() < kBatchJobs) G = g.get();
-    if (!G) {
-      P->groups.push_back(std::make_unique<PlaneGroup>());
-      G = P->groups.back().get();
-      G->patch_half = D->J.patch_half;
-      G->mode = D->J.src_mode;
+  auto group = [&](const std::vector<JobData*>& list, std::vector<std::unique_ptr<PlaneGroup>>& groups) {
+    for (JobData* D : list) {
+      PlaneGroup* G = nullptr;
+      if (!P->per_view)
+        for (auto& g : groups)
+          if (g->patch_half == D->J.patch_half && g->mode == D->J.src_mode && g->nj() < kBatchJobs) G = g.get();
+      if (!G) {
+        groups.push_back(std::make_unique<PlaneGroup>());
+        G = groups.back().get();
+        G->patch_half = D->J.patch_half;
+        G->mode = D->J.src_mode;
+      }
+      G->jobs.push_back(D);
     }
-    G->jobs.push_back(D);
-  }
-  for (auto& g : P->groups) build_group(C, *g);
-  for (auto& g : P->groups) tune_group(C, *g);
+    for (auto& g : groups) build_group(C, *g);
+    for (auto& g : groups) tune_group(C, *g);
+  };
+  std::vector<JobData*> coarse;
+  for (JobData* D : jobs)
+    if (D->coarse) coarse.push_back(D->coarse.get());
+  group(coarse, P->coarse_groups);
+  group(jobs, P->groups);
   if (!P->per_view)
     for (int stage = 0; stage < 3; ++stage) capture_stage(C, *P, stage);
   else

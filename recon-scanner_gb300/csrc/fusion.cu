@@ -331,6 +331,38 @@ __global__ void k_binomial(const uint8_t* __restrict__ in_u8, const float* __res
   out[(size_t)y * w + x] = acc;
 }
 
+// Pyramid level 1: each pixel the mean of a 2 x 2 block of the staged image
+// (8-bit or FP32), so that level-1 pixel centre i + 0.5 is level-0
+// coordinate 2 i + 1 (focal lengths and principal point halve).
+__global__ void k_half_level(const uint8_t* __restrict__ in_u8, const float* __restrict__ in_f32, int w, int h,
+                             int w1, int h1, float* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w1 || y >= h1) return;
+  const size_t i0 = (size_t)(2 * y) * w + 2 * x, i1 = i0 + w;
+  float a, b, c, d;
+  if (in_u8) {
+    a = in_u8[i0];
+    b = in_u8[i0 + 1];
+    c = in_u8[i1];
+    d = in_u8[i1 + 1];
+  } else {
+    a = in_f32[i0];
+    b = in_f32[i0 + 1];
+    c = in_f32[i1];
+    d = in_f32[i1 + 1];
+  }
+  out[(size_t)y * w1 + x] = 0.25f * ((a + b) + (c + d));
+}
+
+cudaError_t launch_half_level(const uint8_t* in_u8, const float* in_f32, int w, int h, float* out, cudaStream_t st) {
+  const int w1 = w / 2, h1 = h / 2;
+  if (w1 < 1 || h1 < 1) return cudaErrorInvalidValue;
+  const dim3 b(32, 8);
+  k_half_level<<<dim3((w1 + 31) / 32, (h1 + 7) / 8), b, 0, st>>>(in_u8, in_f32, w, h, w1, h1, out);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // exclusive scan of uint32 (three-phase, recursive over block sums)
 // ---------------------------------------------------------------------------

@@ -162,6 +162,8 @@ cudaError_t launch_ncc_windows(const uint8_t* ref, int ref_w, int ref_h, const u
                                int patch_size, int n, const NccWindow* win, int* valid, double* ncc, int* weak,
                                int* samples, cudaStream_t st);
 
+// pyramid level 1 of a staged image (w / 2 x h / 2 FP32 means of 2 x 2 blocks)
+cudaError_t launch_half_level(const uint8_t* in_u8, const float* in_f32, int w, int h, float* out, cudaStream_t st);
 // ---- fusion ----
 cudaError_t launch_cloud_finish(const double* pos, const float* conf, unsigned int n, float* weights, double* bounds,
                                 cudaStream_t st);

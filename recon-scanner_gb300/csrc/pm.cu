@@ -321,6 +321,17 @@ __device__ __forceinline__ bool pixel_item(const PlaneBatch& B, int* job, int* x
   return *x < B.jobs[j].w && *y < B.jobs[j].h;
 }
 
+// A neighbour's plane {rho_n at its ray (rxn, ryn), n} carried to the ray
+// (rx, ry): the inverse depth at which that ray meets the plane, or -1 when
+// the plane does not face the camera along either ray.
+__device__ __forceinline__ void plane_candidate_transfer(const float4 hn, float rxn, float ryn, float rx, float ry,
+                                                         float* rho) {
+  // the neighbour's plane n . X = kappa_n / rho_n, evaluated on this pixel's ray
+  const float kn = hn.y * rxn + hn.z * ryn + hn.w;
+  const float kp = hn.y * rx + hn.z * ry + hn.w;
+  *rho = (kn < 0.f && kp < 0.f) ? hn.x * kp / kn : -1.0f;
+}
+
 // Random initialisation (and seed cells) + initial cost.  Block 0 also zeroes
 // the work counters of the persistent sweeps that follow, and each job's
 // first pixel zeroes its filled counter.
@@ -343,6 +354,23 @@ __global__ void __launch_bounds__(128, 4) k_plane_init(const __grid_constant__ P
   float rho = J.rho_min + (J.rho_max - J.rho_min) * g.uniform();
   float nx, ny, nz;
   random_normal(g, rx, ry, &nx, &ny, &nz);
+  if (J.coarse_hyp) {
+    // the parent's plane at the half-resolution level, carried to this ray
+    const int px = min(x >> 1, J.coarse_w - 1), py = min(y >> 1, J.coarse_h - 1);
+    const int pi = py * J.coarse_w + px;
+    if (J.coarse_cost[pi] < kCostInf) {
+      const float4 hn = J.coarse_hyp[pi];
+      float rt;
+      plane_candidate_transfer(hn, ((float)px + 0.5f - J.crcx) / J.crfx, ((float)py + 0.5f - J.crcy) / J.crfy, rx,
+                               ry, &rt);
+      if (rt >= J.rho_min && rt <= J.rho_max) {
+        rho = rt;
+        nx = hn.y;
+        ny = hn.z;
+        nz = hn.w;
+      }
+    }
+  }
   if (J.seed_depth) {
     const int cx = min(x / 32, J.seed_gx - 1);
     const int cy = y / 32;
@@ -375,13 +403,6 @@ __constant__ signed char c_near[4][7][2] = {
     {{-1, 0}, {-2, -1}, {-2, 1}, {-3, -2}, {-3, 2}, {-4, -3}, {-4, 3}},
     {{1, 0}, {2, -1}, {2, 1}, {3, -2}, {3, 2}, {4, -3}, {4, 3}}};
 
-__device__ __forceinline__ void plane_candidate_transfer(const float4 hn, float rxn, float ryn, float rx, float ry,
-                                                         float* rho) {
-  // the neighbour's plane n . X = kappa_n / rho_n, evaluated on this pixel's ray
-  const float kn = hn.y * rxn + hn.z * ryn + hn.w;
-  const float kp = hn.y * rx + hn.z * ry + hn.w;
-  *rho = (kn < 0.f && kp < 0.f) ? hn.x * kp / kn : -1.0f;
-}
 
 // Reference-window statistics from the shared tile (same values as
 // ref_window for pixels whose window lies inside the image).
@@ -636,11 +657,11 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
         const float* plane1 = tile + box_rows * kTileCols;
         const TileRef ref{parity ? plane1 : plane0, parity ? plane0 : plane1, pair, parity, ty};
         const RefWindow rw = tile_window<H>(J, ref, x, y);
-        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
+        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter + J.iter_offset);
       } else {
         const GlobalRef ref{J.pref, J.w, x, y};
         const RefWindow rw = ref_window(J, x, y, J.half_pixel);
-        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter);
+        sweep_pixel<H, kMode>(J, pc, ref, rw, x, y, color, iter + J.iter_offset);
       }
     }
     __syncthreads();

@@ -1,0 +1,93 @@
+"""GPU: coarse-to-fine initialisation (options.coarse_iterations): the first
+iterations run on the half-resolution pyramid level (2x2 means of the staged
+images, halved intrinsics) and the full-resolution search starts from the
+planes found there -- the reference design's search layout (level 1 for the
+coarse rounds, level 0 for the fine ones).
+
+Bar: the batched form equals one launch per view bit for bit with the
+pyramid on; the map is as accurate as the full-resolution search with the
+same total iteration count (median and 95th-percentile relative depth error
+within 5 % of it or better) on the 640x480 sphere scene and a reduced
+tabletop capture; a job too small for the half level runs without it.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mvs():
+    import recon_mvs
+
+    recon_mvs.load_library()
+    return recon_mvs
+
+
+def rel_stats(depth, truth):
+    e = np.abs(depth.astype(np.float64) - truth) / truth
+    r = e[np.isfinite(e)]
+    return float(np.median(r)), float(np.quantile(r, 0.95))
+
+
+def run(mvs, scenes, cfgs, **kw):
+    d = dict(mode=mvs.MODE_PLANE, best_k=4, storage=mvs.STORAGE_FP16, interp=1, refine=2, device=0)
+    d.update(kw)
+    eng = mvs.Engine(mvs.Options(**d))
+    try:
+        jobs = [eng.stage(mvs.ViewArgs.from_cameras(sc.ref.image, [s.image for s in sc.sources], sc.ref.camera,
+                                                    [s.camera for s in sc.sources]), c, undistort=True)
+                for sc, c in zip(scenes, cfgs)]
+        eng.run_many(jobs)
+        return [eng.download(j) for j in jobs]
+    finally:
+        eng.close()
+
+
+def test_pyramid_batched_equals_per_view(mvs):
+    import synthetic as S
+
+    cap = S.tabletop(width=320, height=240, f=1450.0 * 320 / 1920, num_sources=4, seed=6)
+    scenes = [S.as_reference(cap, k) for k in (0, 2, 3)]
+    cfgs = [mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=5, patch_size=11)
+            for sc in scenes]
+    a = run(mvs, scenes, cfgs, coarse_iterations=2)
+    b = run(mvs, scenes, cfgs, coarse_iterations=2, per_view=1)
+    for x, y in zip(a, b):
+        assert x.filled > 0.9 * x.depth.size
+        np.testing.assert_array_equal(x.depth, y.depth)
+        np.testing.assert_array_equal(x.normal, y.normal)
+        np.testing.assert_array_equal(x.cost, y.cost)
+
+
+@pytest.mark.parametrize("scene", ["sphere640", "tabletop960"])
+def test_pyramid_accuracy(mvs, scene):
+    import synthetic as S
+
+    if scene == "sphere640":
+        sc = S.sphere_on_backdrop(width=640, height=480, f=600.0, num_sources=4, seed=1)
+        iters = 6
+    else:
+        cap = S.tabletop(width=960, height=720, f=725.0, num_sources=8, seed=2, device="cuda:0")
+        sc = S.as_reference(cap, 4)
+        iters = 8
+    cfg = mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=iters, patch_size=11)
+    full = run(mvs, [sc], [cfg])[0]
+    pyr = run(mvs, [sc], [cfg], coarse_iterations=2)[0]
+    f_med, f_p95 = rel_stats(full.depth, sc.ref.depth)
+    p_med, p_p95 = rel_stats(pyr.depth, sc.ref.depth)
+    print(f"{scene}: full resolution median {f_med:.3e} p95 {f_p95:.3e} | coarse-to-fine median {p_med:.3e} "
+          f"p95 {p_p95:.3e}")
+    assert p_med <= 1e-3
+    assert p_med <= 1.05 * f_med and p_p95 <= 1.05 * f_p95
+    assert np.isfinite(pyr.depth).mean() >= np.isfinite(full.depth).mean() - 0.005
+
+
+def test_pyramid_skipped_for_tiny_images(mvs):
+    import synthetic as S
+
+    sc = S.sphere_on_backdrop(width=64, height=48, f=60.0, num_sources=2, seed=3)
+    cfg = mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=3, patch_size=11)
+    a = run(mvs, [sc], [cfg])[0]
+    b = run(mvs, [sc], [cfg], coarse_iterations=2)[0]
+    np.testing.assert_array_equal(a.depth, b.depth)
