@@ -495,6 +495,45 @@ RECON_API recon_status recon_mvs_geometric_consistency_noalloc(const recon_mvs_d
                                                                float reproj_px_max, int32_t min_views,
                                                                uint8_t* out_count, uint8_t* out_keep, void* stream);
 
+/* ---- TSDF fusion (the RGBD branch) ----------------------------------------
+ * recon::TsdfVolume (core/include/recon/tsdf_fusion.h:42-98,
+ * core/src/rgbd/tsdf_fusion.cpp) with its grid in device memory: the same
+ * dense grid, the same per-pixel ray walk and running weighted mean, applied
+ * in the reference's order, so grids and extracted points are bit-identical
+ * to the reference's. */
+/* TsdfConfig (tsdf_fusion.h:17-39), field for field. */
+typedef struct recon_tsdf_config {
+  double voxel_size_m, truncation_m, min_depth_m, max_depth_m;
+  double fx, fy, cx, cy;
+  double origin_x, origin_y, origin_z;
+  double bbox_max_x, bbox_max_y, bbox_max_z;
+  int32_t min_confidence;
+} recon_tsdf_config;
+RECON_API recon_status recon_tsdf_config_default(recon_tsdf_config* out);
+/* TsdfVolume::TsdfVolume: a grid of FloorToIntScaled(extent / voxel) + 1
+ * voxels per axis on `device` (tsdf 1, weight 0); at most 2^31 voxels. */
+RECON_API recon_status recon_tsdf_create(const recon_tsdf_config* cfg, int32_t device, void** out_volume);
+/* TsdfVolume::IntegrateDepthFrame (tsdf_fusion.h:54-57): host depth in
+ * uint16 millimetres of axial depth, optional uint8 confidence,
+ * world_to_camera 4 x 4 row-major; *out_integrated = the pixels fused.
+ * Synchronises. */
+RECON_API recon_status recon_tsdf_integrate(void* volume, const uint16_t* depth_mm, const uint8_t* confidence,
+                                            int32_t width, int32_t height, const double* world_to_camera,
+                                            float depth_uncertainty_m, uint32_t* out_integrated);
+/* TsdfVolume::ExtractPoints (tsdf_fusion.h:60-62): zero-crossing voxels in
+ * (iz, iy, ix) order -- positions, normals, confidences; keys = linear voxel
+ * index, counts = 1, colours 0 (freed with recon_mvs_point_cloud_free). */
+RECON_API recon_status recon_tsdf_extract_points(void* volume, recon_mvs_point_cloud* out);
+/* TsdfVolume::dims (x, y, z) and MemoryUsageBytes (the device grid: 8 bytes a
+ * voxel; the reference also counts 12 bytes of colour it never writes). */
+RECON_API recon_status recon_tsdf_dims(void* volume, int32_t* out_dims);
+RECON_API recon_status recon_tsdf_memory_usage(void* volume, uint64_t* out_bytes);
+/* Copies of the grid (nx * ny * nz floats each, index (iz * ny + iy) * nx +
+ * ix; either may be NULL).  No counterpart in the reference, whose grid is
+ * private. */
+RECON_API recon_status recon_tsdf_read_grid(void* volume, float* tsdf, float* weight);
+RECON_API void recon_tsdf_destroy(void* volume);
+
 /* Human-readable description of the last error on this thread. */
 RECON_API const char* recon_mvs_last_error(void);
 

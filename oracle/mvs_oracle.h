@@ -266,6 +266,28 @@ void orc_undistort(const uint8_t* img, int32_t w, int32_t h, const orc_intrinsic
 /* BgraToGray (orchestrator.cpp:53-67): BT.601 integer weights. */
 void orc_bgra_to_gray(const uint8_t* bgra, int32_t w, int32_t h, int32_t stride, uint8_t* out);
 
+/* ---- TSDF fusion (core/src/rgbd/tsdf_fusion.cpp, tsdf_internal.h) ---- */
+/* TsdfConfig (core/include/recon/tsdf_fusion.h:17-39), field for field. */
+typedef struct orc_tsdf_config {
+  double voxel_size_m, truncation_m, min_depth_m, max_depth_m;
+  double fx, fy, cx, cy;
+  double origin_x, origin_y, origin_z;
+  double bbox_max_x, bbox_max_y, bbox_max_z;
+  int32_t min_confidence;
+} orc_tsdf_config;
+/* TsdfVolume's grid dimensions (x, y, z). */
+void orc_tsdf_dims(const orc_tsdf_config* cfg, int32_t dims[3]);
+/* TsdfVolume::IntegrateDepthFrame on grid arrays (index (iz * ny + iy) * nx
+ * + ix; tsdf starts at 1, weight at 0); w2c row-major 4 x 4.  Returns the
+ * pixels fused. */
+uint32_t orc_tsdf_integrate(const orc_tsdf_config* cfg, float* tsdf, float* weight, const uint16_t* depth_mm,
+                            const uint8_t* confidence, int32_t width, int32_t height, const double w2c[16],
+                            float depth_uncertainty_m);
+/* TsdfVolume::ExtractPoints: returns the count, writes at most `cap`
+ * (positions / normals 3 per point, confidence, optional voxel index). */
+int64_t orc_tsdf_extract(const orc_tsdf_config* cfg, const float* tsdf, const float* weight, int64_t cap,
+                         double* pos, double* nrm, float* conf, int64_t* voxel_index);
+
 #ifdef __cplusplus
 }
 #endif

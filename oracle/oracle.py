@@ -257,6 +257,15 @@ def load(which: str = "oracle") -> "Checker":
         lib.orc_plane_patchmatch_ex.restype = C.c_uint32
         lib.orc_plane_patchmatch_ex.argtypes = [V, P, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
                                                 C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.orc_tsdf_dims.argtypes = [C.POINTER(TsdfConfig), C.POINTER(C.c_int32)]
+        lib.orc_tsdf_integrate.restype = C.c_uint32
+        lib.orc_tsdf_integrate.argtypes = [C.POINTER(TsdfConfig), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.POINTER(C.c_uint16), C.POINTER(C.c_uint8), C.c_int32, C.c_int32,
+                                           C.POINTER(C.c_double), C.c_float]
+        lib.orc_tsdf_extract.restype = C.c_int64
+        lib.orc_tsdf_extract.argtypes = [C.POINTER(TsdfConfig), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                         C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_float), C.POINTER(C.c_int64)]
         lib.orc_bgra_to_gray.argtypes = [C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
                                          C.POINTER(C.c_uint8)]
         lib.orc_xorshift_next.restype = C.c_uint32
@@ -270,6 +279,112 @@ def load(which: str = "oracle") -> "Checker":
     chk = Checker(lib, prefix)
     _LIBS[which] = chk
     return chk
+
+
+# ---- TSDF fusion (core/src/rgbd/tsdf_fusion.cpp) ----
+REF_TSDF_SO = os.path.join(HERE, "_ref", "libref_tsdf.so")
+
+# TsdfConfig (core/include/recon/tsdf_fusion.h:17-39), defaults included.
+_TSDF_FIELDS = [("voxel_size_m", C.c_double, 0.001), ("truncation_m", C.c_double, 0.008),
+                ("min_depth_m", C.c_double, 0.05), ("max_depth_m", C.c_double, 3.0), ("fx", C.c_double, 1.0),
+                ("fy", C.c_double, 1.0), ("cx", C.c_double, 0.0), ("cy", C.c_double, 0.0),
+                ("origin_x", C.c_double, 0.0), ("origin_y", C.c_double, 0.0), ("origin_z", C.c_double, 0.0),
+                ("bbox_max_x", C.c_double, 1.0), ("bbox_max_y", C.c_double, 1.0), ("bbox_max_z", C.c_double, 1.0),
+                ("min_confidence", C.c_int32, 30)]
+TSDF_DEFAULTS = {n: d for n, _, d in _TSDF_FIELDS}
+
+
+class TsdfConfig(C.Structure):
+    _fields_ = [(n, t) for n, t, _ in _TSDF_FIELDS]
+
+
+def tsdf_config(**overrides) -> TsdfConfig:
+    unknown = set(overrides) - set(TSDF_DEFAULTS)
+    if unknown:
+        raise KeyError(f"unknown TsdfConfig fields: {sorted(unknown)}")
+    c = TsdfConfig()
+    for n, _, d in _TSDF_FIELDS:
+        setattr(c, n, overrides.get(n, d))
+    return c
+
+
+def _tsdf_frames(frames):
+    """frames: list of (depth uint16 HxW, confidence uint8 HxW or None, w2c
+    4x4, depth uncertainty) -> stacked arrays."""
+    depth = np.ascontiguousarray(np.stack([f[0] for f in frames]), np.uint16)
+    has_conf = frames[0][1] is not None
+    conf = np.ascontiguousarray(np.stack([f[1] for f in frames]), np.uint8) if has_conf else None
+    w2c = np.ascontiguousarray(np.stack([np.asarray(f[2], np.float64).reshape(4, 4) for f in frames]), np.float64)
+    unc = np.ascontiguousarray([f[3] for f in frames], np.float32)
+    return depth, conf, w2c, unc
+
+
+def tsdf_dims(cfg: TsdfConfig):
+    lib = load("oracle").lib
+    d = (C.c_int32 * 3)()
+    lib.orc_tsdf_dims(C.byref(cfg), d)
+    return tuple(int(v) for v in d)
+
+
+def tsdf_fuse(cfg: TsdfConfig, frames):
+    """The oracle: TsdfVolume::IntegrateDepthFrame over the frames, then
+    ExtractPoints.  Returns dict(tsdf, weight (nz, ny, nx), integrated,
+    positions, normals, confidences, voxel_index)."""
+    lib = load("oracle").lib
+    nx, ny, nz = tsdf_dims(cfg)
+    tsdf = np.ones((nz, ny, nx), np.float32)
+    weight = np.zeros((nz, ny, nx), np.float32)
+    integ = []
+    for dep, cf_, m, u in frames:  # frame by frame: a frame may have no confidence map
+        dep = np.ascontiguousarray(dep, np.uint16)
+        cf_ = None if cf_ is None else np.ascontiguousarray(cf_, np.uint8)
+        m = np.ascontiguousarray(np.asarray(m, np.float64).reshape(4, 4))
+        h, w = dep.shape
+        integ.append(int(lib.orc_tsdf_integrate(C.byref(cfg), _ptr(tsdf, C.c_float), _ptr(weight, C.c_float),
+                                                _ptr(dep, C.c_uint16), _ptr(cf_, C.c_uint8) if cf_ is not None else None,
+                                                w, h, _ptr(m, C.c_double), float(u))))
+    n = int(lib.orc_tsdf_extract(C.byref(cfg), _ptr(tsdf, C.c_float), _ptr(weight, C.c_float), 0, None, None, None,
+                                 None))
+    pos = np.zeros((max(n, 1), 3))
+    nrm = np.zeros((max(n, 1), 3))
+    cf = np.zeros(max(n, 1), np.float32)
+    vi = np.zeros(max(n, 1), np.int64)
+    lib.orc_tsdf_extract(C.byref(cfg), _ptr(tsdf, C.c_float), _ptr(weight, C.c_float), n, _ptr(pos, C.c_double),
+                         _ptr(nrm, C.c_double), _ptr(cf, C.c_float), _ptr(vi, C.c_int64))
+    return dict(tsdf=tsdf, weight=weight, integrated=integ, positions=pos[:n], normals=nrm[:n], confidences=cf[:n],
+                voxel_index=vi[:n])
+
+
+def tsdf_reference(cfg: TsdfConfig, frames):
+    """The reference's own TSDF code (libref_tsdf.so): dict(tsdf, weight,
+    integrated, positions, normals, confidences)."""
+    if not os.path.exists(REF_TSDF_SO):
+        build_oracle(ref=True)
+    lib = C.CDLL(REF_TSDF_SO)
+    nx, ny, nz = tsdf_dims(cfg)
+    depth, conf, w2c, unc = _tsdf_frames(frames)
+    nf, h, w = depth.shape
+    tsdf = np.ones((nz, ny, nx), np.float32)
+    weight = np.zeros((nz, ny, nx), np.float32)
+    cptr = _ptr(conf, C.c_uint8) if conf is not None else None
+    lib.ref_tsdf_grid.argtypes = [C.POINTER(TsdfConfig), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.ref_tsdf_grid(C.byref(cfg), nf, depth.ctypes.data, conf.ctypes.data if conf is not None else None, w, h,
+                      w2c.ctypes.data, unc.ctypes.data, tsdf.ctypes.data, weight.ctypes.data)
+    cap = nx * ny * nz
+    pos = np.zeros((cap, 3))
+    nrm = np.zeros((cap, 3))
+    cf = np.zeros(cap, np.float32)
+    integ = np.zeros(nf, np.uint32)
+    lib.ref_tsdf_run.restype = C.c_int64
+    lib.ref_tsdf_run.argtypes = [C.POINTER(TsdfConfig), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    n = int(lib.ref_tsdf_run(C.byref(cfg), nf, depth.ctypes.data, conf.ctypes.data if conf is not None else None, w,
+                             h, w2c.ctypes.data, unc.ctypes.data, integ.ctypes.data, cap, pos.ctypes.data,
+                             nrm.ctypes.data, cf.ctypes.data))
+    del cptr
+    return dict(tsdf=tsdf, weight=weight, integrated=[int(v) for v in integ], positions=pos[:n], normals=nrm[:n],
+                confidences=cf[:n])
 
 
 def reference_available() -> bool:

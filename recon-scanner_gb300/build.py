@@ -19,7 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librecon_mvs_gb300.so")
-SOURCES = ["engine.cu", "pm.cu", "fusion.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["engine.cu", "pm.cu", "fusion.cu", "noalloc.cu", "adjoint.cu", "tsdf.cu"]
 HEADERS = ["common.cuh", "cost.cuh", "kernels.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

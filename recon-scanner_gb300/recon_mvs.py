@@ -126,6 +126,22 @@ class DeviceCloudC(C.Structure):
                 ("impl", C.c_void_p)]
 
 
+class TsdfConfig(C.Structure):
+    """recon::TsdfConfig (tsdf_fusion.h:17-39); TsdfConfig() has the reference defaults."""
+
+    _fields_ = [("voxel_size_m", C.c_double), ("truncation_m", C.c_double), ("min_depth_m", C.c_double),
+                ("max_depth_m", C.c_double), ("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double),
+                ("cy", C.c_double), ("origin_x", C.c_double), ("origin_y", C.c_double), ("origin_z", C.c_double),
+                ("bbox_max_x", C.c_double), ("bbox_max_y", C.c_double), ("bbox_max_z", C.c_double),
+                ("min_confidence", C.c_int32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        _lib().recon_tsdf_config_default(C.byref(self))
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
 class Stats(C.Structure):
     _fields_ = [("hypotheses_evaluated", C.c_uint64), ("last_run_ms", C.c_double), ("last_sweep_ms", C.c_double),
                 ("last_sweep_launches", C.c_int32), ("tile_rows", C.c_int32), ("ctas_per_sm", C.c_int32),
@@ -214,6 +230,15 @@ _SIGS = {
                                              C.POINTER(C.c_int32)]),
     "recon_mvs_device_cloud_download": (C.c_int, [C.c_void_p, C.POINTER(DeviceCloudC), C.POINTER(PointCloudC)]),
     "recon_mvs_device_cloud_free": (None, [C.POINTER(DeviceCloudC)]),
+    "recon_tsdf_config_default": (C.c_int, [C.c_void_p]),
+    "recon_tsdf_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "recon_tsdf_integrate": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint16), C.POINTER(C.c_uint8), C.c_int32,
+                                       C.c_int32, C.POINTER(C.c_double), C.c_float, C.POINTER(C.c_uint32)]),
+    "recon_tsdf_extract_points": (C.c_int, [C.c_void_p, C.POINTER(PointCloudC)]),
+    "recon_tsdf_dims": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "recon_tsdf_memory_usage": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "recon_tsdf_read_grid": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "recon_tsdf_destroy": (None, [C.c_void_p]),
     "recon_mvs_job_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -737,3 +762,55 @@ class Engine:
 
 def exported_symbols():
     return list(_SIGS)
+
+
+class TsdfVolume:
+    """recon::TsdfVolume (tsdf_fusion.h:42-98) with its grid in device memory."""
+
+    def __init__(self, config: TsdfConfig, device: int = 0):
+        self.ptr = C.c_void_p()
+        _check(_lib().recon_tsdf_create(C.byref(config), device, C.byref(self.ptr)))
+
+    def IntegrateDepthFrame(self, depth_mm, confidence, world_to_camera, depth_uncertainty_m) -> int:
+        d = np.ascontiguousarray(depth_mm, np.uint16)
+        c = None if confidence is None else np.ascontiguousarray(confidence, np.uint8)
+        m = np.ascontiguousarray(np.asarray(world_to_camera, np.float64).reshape(4, 4))
+        n = C.c_uint32()
+        _check(_lib().recon_tsdf_integrate(self.ptr, _ptr(d, C.c_uint16), _ptr(c, C.c_uint8) if c is not None else None,
+                                           d.shape[1], d.shape[0], _ptr(m, C.c_double), float(depth_uncertainty_m),
+                                           C.byref(n)))
+        return int(n.value)
+
+    def ExtractPoints(self) -> "PointCloud":
+        pc = PointCloudC()
+        _check(_lib().recon_tsdf_extract_points(self.ptr, C.byref(pc)))
+        return _take_cloud(pc)
+
+    def dims(self):
+        d = (C.c_int32 * 3)()
+        _check(_lib().recon_tsdf_dims(self.ptr, d))
+        return tuple(int(v) for v in d)
+
+    def MemoryUsageBytes(self) -> int:
+        b = C.c_uint64()
+        _check(_lib().recon_tsdf_memory_usage(self.ptr, C.byref(b)))
+        return int(b.value)
+
+    def grid(self):
+        """(tsdf, weight) as (nz, ny, nx) FP32 host arrays."""
+        nx, ny, nz = self.dims()
+        t = np.zeros((nz, ny, nx), np.float32)
+        w = np.zeros((nz, ny, nx), np.float32)
+        _check(_lib().recon_tsdf_read_grid(self.ptr, _ptr(t, C.c_float), _ptr(w, C.c_float)))
+        return t, w
+
+    def close(self):
+        if self.ptr:
+            _lib().recon_tsdf_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 -- interpreter shutdown
+            pass

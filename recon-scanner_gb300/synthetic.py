@@ -492,3 +492,79 @@ def plane_test_scene(width=160, height=120, f=400.0, num_views=5, baseline=0.016
         ty = lround(p[..., 1] * 1500.0) + 512
         images.append(texture(tx, ty))
     return images, cams, truth
+
+
+# ----------------------------------------------------------------------------
+# RGBD depth frames for TSDF fusion
+# ----------------------------------------------------------------------------
+
+def tsdf_pose(tx: float, ty: float, tz: float, yaw: float) -> np.ndarray:
+    """4x4 world -> camera transform: a rotation about y by `yaw` and a
+    translation (the reference TSDF test's pose family,
+    tests/unit/test_tsdf_tiled.cpp:82-90)."""
+    c, s = math.cos(yaw), math.sin(yaw)
+    m = np.eye(4)
+    m[0, 0], m[0, 2], m[2, 0], m[2, 2] = c, s, -s, c
+    m[:3, 3] = (tx, ty, tz)
+    return m
+
+
+def tilted_wall_frames():
+    """The reference TSDF test's scene (tests/unit/test_tsdf_tiled.cpp:38-60,
+    62-80, 134-138): a 160 x 160 depth frame of the plane
+    z = 0.5 + 0.05 x_norm, confidence 220, fused from three poses; its
+    TsdfConfig as a dict."""
+    w = h = 160
+    u = np.arange(w)
+    x_norm = (2.0 * u / (w - 1)) - 1.0
+    z = 0.5 + 0.05 * x_norm
+    row = np.floor(z * 1000.0 + 0.5).astype(np.uint16)  # lround of positive values
+    depth = np.tile(row, (h, 1))
+    conf = np.full((h, w), 220, np.uint8)
+    poses = [tsdf_pose(0.0, 0.0, 0.0, 0.0), tsdf_pose(0.03, 0.01, 0.0, 0.05), tsdf_pose(-0.02, 0.0, 0.0, -0.04)]
+    cfg = dict(voxel_size_m=0.004, truncation_m=0.02, min_depth_m=0.05, max_depth_m=2.0, fx=180.0, fy=180.0, cx=80.0,
+               cy=80.0, origin_x=-0.30, origin_y=-0.20, origin_z=0.30, bbox_max_x=0.30, bbox_max_y=0.20,
+               bbox_max_z=0.70, min_confidence=30)
+    return cfg, [(depth, conf, p, 0.004) for p in poses]
+
+
+def tsdf_capture(width=320, height=240, f=300.0, n_frames=4, seed=0, voxel=0.002, truncation=0.008,
+                 holes=0.02, low_confidence=0.05):
+    """Depth frames of a sphere (r = 50 mm, centre 0.35 m ahead) in front of
+    a wall at 0.45 m, as an RGBD sensor reports them: uint16 millimetres of
+    axial depth for the TSDF convention (pixel index = image coordinate, ray
+    ((u - cx) / fx, (v - cy) / fy, 1)), Gaussian depth noise growing with
+    depth, a seeded share of holes (0) and of confidences below the default
+    threshold of 30; poses from tsdf_pose around the first camera; each frame
+    with its own depth uncertainty.  Returns (TsdfConfig dict covering the
+    scene, frames)."""
+    rng = np.random.default_rng(seed)
+    cx, cy = width / 2.0, height / 2.0
+    v, u = np.mgrid[0:height, 0:width].astype(np.float64)
+    dcam = np.stack([(u - cx) / f, (v - cy) / f, np.ones_like(u)], -1)
+    frames = []
+    for i in range(n_frames):
+        yaw = rng.uniform(-0.08, 0.08)
+        w2c = tsdf_pose(rng.uniform(-0.02, 0.02), rng.uniform(-0.015, 0.015), rng.uniform(-0.01, 0.01), yaw)
+        R, t = w2c[:3, :3], w2c[:3, 3]
+        cen = -R.T @ t
+        dw = dcam @ R  # R^T d per pixel
+        tz = (0.45 - cen[2]) / dw[..., 2]
+        oc = cen - np.array([0.0, 0.0, 0.35])
+        b = dw @ oc
+        a = (dw * dw).sum(-1)
+        cc = oc @ oc - 0.05 ** 2
+        disc = b * b - a * cc
+        ts = np.where(disc >= 0, (-b - np.sqrt(np.maximum(disc, 0.0))) / a, np.inf)
+        z = np.where((ts > 0) & (ts < tz), ts, tz)  # camera z = t for d_z = 1
+        z = z * (1.0 + rng.normal(0.0, 0.0005, z.shape))
+        depth = np.clip(np.floor(z * 1000.0 + 0.5), 0, 65535).astype(np.uint16)
+        depth[rng.random(depth.shape) < holes] = 0
+        conf = rng.integers(30, 256, depth.shape).astype(np.uint8)
+        low = rng.random(depth.shape) < low_confidence
+        conf[low] = rng.integers(0, 30, int(low.sum())).astype(np.uint8)
+        frames.append((depth, conf, w2c, float(rng.uniform(0.002, 0.006))))
+    cfg = dict(voxel_size_m=voxel, truncation_m=truncation, min_depth_m=0.05, max_depth_m=2.0, fx=f, fy=f, cx=cx,
+               cy=cy, origin_x=-0.20, origin_y=-0.16, origin_z=0.26, bbox_max_x=0.20, bbox_max_y=0.16,
+               bbox_max_z=0.50, min_confidence=30)
+    return cfg, frames

@@ -21,6 +21,14 @@ without the reference tree:
   pm_sphere.npz      the same on a 96x72 sphere scene with sparse seeds
   select.npz         SelectSourceViews on the unit test's poses and on a
                      20-pose ring
+  tsdf.npz           TsdfVolume::IntegrateDepthFrame + ExtractPoints (the
+                     reference's tsdf_fusion.cpp, oracle/_ref/libref_tsdf.so)
+                     on the reference TSDF test's tilted wall (3 frames) and
+                     on a 320x240 sphere capture with holes and
+                     low-confidence pixels (4 frames); grids and points
+                     recorded as digests
+
+`python tests/golden/make_golden.py tsdf` writes tsdf.npz alone.
 """
 from __future__ import annotations
 
@@ -236,5 +244,28 @@ def main():
     print("golden vectors written to", HERE)
 
 
+def make_tsdf():
+    scenes = {"wall": S.tilted_wall_frames(), "capture": S.tsdf_capture()}
+    out = {}
+    for name, (cfgd, frames) in scenes.items():
+        cfg = O.tsdf_config(**cfgd)
+        r = O.tsdf_reference(cfg, frames)
+        out[name + "_cfg"] = np.array([[k, repr(v)] for k, v in cfgd.items()])
+        out[name + "_depth"] = np.stack([f[0] for f in frames])
+        out[name + "_conf"] = np.stack([f[1] for f in frames])
+        out[name + "_w2c"] = np.stack([np.asarray(f[2], np.float64) for f in frames])
+        out[name + "_unc"] = np.asarray([f[3] for f in frames], np.float32)
+        out[name + "_integrated"] = np.asarray(r["integrated"], np.int64)
+        out[name + "_grid_digest"] = digest(r["tsdf"], r["weight"])
+        out[name + "_fused_voxels"] = int((r["weight"] > 0).sum())
+        out.update(cloud_fields(name + "_", r["positions"], r["normals"], r["confidences"]))
+    np.savez_compressed(os.path.join(HERE, "tsdf.npz"), **out)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["tsdf"]:
+        make_tsdf()
+        print("tsdf.npz written to", HERE)
+        sys.exit(0)
     main()
+    make_tsdf()
