@@ -398,6 +398,15 @@ def run_reference_arm(args):
             "cpu_baseline": {"value": value, "unit": "depth maps/s", "cores": smp.threads, "kind": smp.kind,
                              "sample": smp.describe(len(runs), measured)},
             "e2e": {"value": value, "unit": "depth maps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if WORKLOAD == "c2":
+        # one whole map 0 timed once against the tile estimate of the same
+        # host (profiles/reference_cpu_tabletop1920.md)
+        line["extrapolation_check"] = {
+            "full_map_s": 3216.1, "tile_estimate_s_48_tiles": 2739.4, "rel_err_48_tiles": -0.148,
+            "rel_err_4_10_20_tiles": [-0.306, -0.221, -0.240],
+            "host": "8 x86 Xeon threads (the build host), the reference's release build",
+            "reading": "the tile samples under-estimate a whole map by 15-30 %: the reference arm's speed is "
+                       "if anything too high, so GPU / CPU ratios from it are conservative"}
     print(json.dumps(line))
 
 
