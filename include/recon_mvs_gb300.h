@@ -462,6 +462,12 @@ RECON_API void recon_mvs_device_cloud_free(recon_mvs_device_cloud* cloud);
 RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_depth_map* out,
                                               uint32_t* out_filled);
 RECON_API recon_status recon_mvs_job_release(void* ctx, int32_t job);
+/* Test hook for the failure path of the sweep's bounded tile waits: the
+ * next plane-mode run of this context issues no reference-tile copy and
+ * waits at most 4096 polls for each, so every wait runs out; the run's
+ * download then returns RECON_ERR_MVS_GPU_FAILURE and the context stays
+ * usable (the following run is normal).  No counterpart in the reference. */
+RECON_API recon_status recon_mvs_test_inject_tma_timeout(void* ctx);
 RECON_API recon_status recon_mvs_synchronize(void* ctx);
 RECON_API recon_status recon_mvs_context_stats(void* ctx, recon_mvs_stats* out);
 /* Geometric consistency for callers that cannot let a library allocate

@@ -292,6 +292,7 @@ struct Context {
   int next_image = 1;
   DevArray<unsigned long long> counter;
   DevArray<int> err;  // device-side failure flag (a TMA wait that ran out)
+  bool test_tma_timeout = false;  // the next plane run injects a TMA wait that runs out
   DevArray<uint8_t> stage_u8;
   DevArray<float> stage_f32;
   DevArray<uint8_t> stage_tex;
@@ -942,6 +943,8 @@ static void build_group(Context& C, PlaneGroup& G) {
   G.pix->err = C.err.p;
   for (int r = 0; r < kNumRowChoices; ++r) {
     G.sweep[r]->err = C.err.p;
+    G.sweep[r]->tma_skip = C.test_tma_timeout ? 1 : 0;
+    G.sweep[r]->tma_poll_limit = C.test_tma_timeout ? 4096 : 0;
     if (G.patch_half != 5 && G.patch_half != 3) continue;  // the generic window reads global memory
     std::vector<CUtensorMap> maps(n);
     for (int j = 0; j < n; ++j) encode_ref_tile_map(*G.jobs[j], kRowChoices[r] + 2 * G.patch_half, &maps[j]);
@@ -1142,12 +1145,20 @@ static std::unique_ptr<PlanePlan> make_plan(Context& C, const std::vector<JobDat
 
 static void run_plane_jobs(Context& C, const std::vector<JobData*>& jobs, const std::vector<int>& ids) {
   if (jobs.empty()) return;
-  if (!C.plan || C.plan->ids != ids || C.plan->per_view != (C.opts.per_view != 0)) {
+  if (!C.plan || C.plan->ids != ids || C.plan->per_view != (C.opts.per_view != 0) || C.test_tma_timeout) {
     C.plan.reset();
     C.plan = make_plan(C, jobs, ids);
   }
   PlanePlan& P = *C.plan;
   launch_plan(C, P);
+  if (C.test_tma_timeout) {
+    // the injection lasts one run: the next run rebuilds its plan
+    CK(cudaStreamSynchronize(C.stream));
+    C.test_tma_timeout = false;
+    C.plan.reset();
+    C.stats.last_sweep_launches = 0;
+    return;
+  }
   if (P.exec[0]) C.stats.graph_launches += 1;
   C.stats.last_sweep_launches = P.sweep_launches;
   C.stats.tile_rows = P.groups[0]->rows;
@@ -2604,6 +2615,13 @@ RECON_API recon_status recon_mvs_job_download(void* ctx, int32_t job, recon_mvs_
     Context& C = *static_cast<Context*>(ctx);
     C.use();
     download_job(C, get_job(C, job), out, filled);
+  });
+}
+
+RECON_API recon_status recon_mvs_test_inject_tma_timeout(void* ctx) {
+  return guard([&] {
+    if (!ctx) fail(RECON_ERR_INVALID_ARGUMENT, "NULL context");
+    static_cast<Context*>(ctx)->test_tma_timeout = true;
   });
 }
 

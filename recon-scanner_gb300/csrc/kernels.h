@@ -117,6 +117,10 @@ struct PlaneBatch {
   // 64-byte aligned), box = kTileCols columns x (rows + 2H) rows x 2 planes
   const CUtensorMap* tmaps;
   int* err;  // set when a TMA wait runs out (the launch then stops early)
+  // fault injection for the test of that path: 1 = issue no tile copy (every
+  // wait runs out); the poll limit of a wait (0 = the default)
+  int tma_skip;
+  int tma_poll_limit;
 };
 static_assert(sizeof(PlaneBatch) + 64 <= 32764, "PlaneBatch exceeds the kernel-parameter limit");
 cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int max_src, int* queues, int num_queues,

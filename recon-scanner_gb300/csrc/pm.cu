@@ -637,16 +637,17 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
     if constexpr (H > 0) {
       // the tile: planes [2][box_rows][kTileCols] of ref_de from column bx*32 - 8 and
       // row by*R - H, one TMA box (zeros outside the image)
-      if (tid == 0)
+      const int polls = B.tma_poll_limit > 0 ? B.tma_poll_limit : kTmaWaitPolls;
+      if (tid == 0 && !B.tma_skip)
         tma_load_3d(tile, B.tmaps + j, bx * 32 - 8, by * R - H, 0, &bar,
                     (uint32_t)(2 * box_rows * kTileCols * sizeof(float)));
-      const bool ok = mbar_wait(&bar, phase, kTmaWaitPolls);
+      const bool ok = mbar_wait(&bar, phase, polls);
       phase ^= 1u;
       if (__syncthreads_or(!ok)) {
         // give the copy one more bounded chance to land before leaving
         if (tid == 0) {
           atomicExch(B.err, 1);
-          mbar_wait(&bar, phase ^ 1u, kTmaWaitPolls);
+          mbar_wait(&bar, phase ^ 1u, polls);
         }
         break;
       }

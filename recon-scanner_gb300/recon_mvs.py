@@ -230,6 +230,7 @@ _SIGS = {
                                              C.POINTER(C.c_int32)]),
     "recon_mvs_device_cloud_download": (C.c_int, [C.c_void_p, C.POINTER(DeviceCloudC), C.POINTER(PointCloudC)]),
     "recon_mvs_device_cloud_free": (None, [C.POINTER(DeviceCloudC)]),
+    "recon_mvs_test_inject_tma_timeout": (C.c_int, [C.c_void_p]),
     "recon_tsdf_config_default": (C.c_int, [C.c_void_p]),
     "recon_tsdf_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "recon_tsdf_integrate": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint16), C.POINTER(C.c_uint8), C.c_int32,
