@@ -91,3 +91,23 @@ def test_pyramid_skipped_for_tiny_images(mvs):
     a = run(mvs, [sc], [cfg])[0]
     b = run(mvs, [sc], [cfg], coarse_iterations=2)[0]
     np.testing.assert_array_equal(a.depth, b.depth)
+
+
+def test_pyramid_mixed_batch(mvs):
+    """One batch mixing sizes, iteration counts and a job too small for the
+    half level (which runs without it): batched equals per-view bit for bit,
+    and the small job's map equals its map run without coarse-to-fine."""
+    import synthetic as S
+
+    cap = S.tabletop(width=320, height=240, f=1450.0 * 320 / 1920, num_sources=3, seed=12)
+    small = S.sphere_on_backdrop(width=80, height=60, f=75.0, num_sources=3, seed=13)
+    scenes = [S.as_reference(cap, 0), small, S.as_reference(cap, 2)]
+    cfgs = [mvs.MvsConfig(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=it, patch_size=11)
+            for sc, it in zip(scenes, (5, 4, 3))]
+    a = run(mvs, scenes, cfgs, coarse_iterations=2)
+    b = run(mvs, scenes, cfgs, coarse_iterations=2, per_view=1)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.depth, y.depth)
+        np.testing.assert_array_equal(x.cost, y.cost)
+    c = run(mvs, [small], [cfgs[1]])[0]
+    np.testing.assert_array_equal(a[1].depth, c.depth)
