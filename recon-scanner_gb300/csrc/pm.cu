@@ -610,12 +610,27 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const PCache pc{smem, nthreads, tid};
   const int box_rows = R + 2 * H;
-  // this thread's pixel in the tile: row ty, same-colour column pair `pair`
+  // this thread's pixel in the tile: row ty, same-colour column pair `pair`.
+  // A warp covers RW rows x PW pairs; within it each quad of lanes (the
+  // texture unit's unit of work) takes 2 rows x 2 pairs -- a compact 4 x 2
+  // pixel diamond whose source footprints share texture-cache sectors --
+  // rather than 4 pairs of one row.
   const int RW = R < 4 ? R : 4;        // rows per warp
   const int PW = 32 / RW;              // pixels per warp row
   const int w = (int)threadIdx.y, l = (int)threadIdx.x;
-  const int ty = (w / RW) * RW + l / PW;
-  const int pair = (w % RW) * PW + l % PW;
+  int r_in, c_in;
+  if (RW == 4) {
+    r_in = ((l >> 4) << 1) | ((l >> 1) & 1);
+    c_in = (((l >> 2) & 3) << 1) | (l & 1);
+  } else if (RW == 2) {
+    r_in = (l >> 1) & 1;
+    c_in = ((l >> 2) << 1) | (l & 1);
+  } else {
+    r_in = 0;
+    c_in = l;
+  }
+  const int ty = (w / RW) * RW + r_in;
+  const int pair = (w % RW) * PW + c_in;
   if constexpr (H > 0) {
     if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
