@@ -572,7 +572,10 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
     steps) in the forms between them -- batched FP32 exact golden section,
     + FP16 storage, + Gauss-Newton (the batched FP16 form with exact
     interpolation) -- beside the plain path and the chosen form (texture-unit
-    interpolation) timed above; each with its accuracy.  And what the
+    interpolation) timed above; each with its accuracy.  The exact
+    Gauss-Newton form is also timed with its windows staged in shared memory
+    (with the fraction of windows read from the boxes and a bit-identity
+    check against its texture reads), alone and with coarse-to-fine.  And what the
     texture unit's 8-bit filter weights cost: the plane cost of 2 x 10^4
     seeded hypotheses on a pinhole copy of the capture's map 0, FP16 storage,
     exact and texture-unit interpolation, against the FP64 oracle (a checker
@@ -581,18 +584,31 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
 
     import synthetic as Syn
 
-    forms = [("batched_fp32_exact_golden", False, 0, 1, 0), ("batched_fp16_exact_golden", True, 0, 1, 0),
-             ("batched_fp16_exact_gauss_newton", True, 0, 2, 0),
-             ("batched_fp16_texture_gauss_newton_full_resolution", True, 1, 2, 0)]
+    # (name, fp16, interp, refine, coarse iterations, window staging: 1 texture reads, 2 staged boxes)
+    forms = [("batched_fp32_exact_golden", False, 0, 1, 0, 1), ("batched_fp16_exact_golden", True, 0, 1, 0, 1),
+             ("batched_fp16_exact_gauss_newton", True, 0, 2, 0, 1),
+             ("batched_fp16_exact_gauss_newton_staged_windows", True, 0, 2, 0, 2),
+             ("batched_fp16_exact_gauss_newton_staged_windows_coarse_to_fine", True, 0, 2, args.coarse, 2),
+             ("batched_fp16_texture_gauss_newton_full_resolution", True, 1, 2, 0, 1)]
     out = {"steps": args.attr_steps, "forms": {}}
-    for name, fp16, interp, refine, coarse in forms:
-        ms, _, _, _, fmaps, _ = time_form(M, views, cfgs, mk(fp16, interp, False, refine, coarse), args.attr_steps, 1,
-                                          flush, world, undistort, scenes=scenes)
+    exact_maps = None
+    for name, fp16, interp, refine, coarse, staging in forms:
+        ms, _, _, _, fmaps, fst = time_form(M, views, cfgs, mk(fp16, interp, False, refine, coarse, staging),
+                                            args.attr_steps, 1, flush, world, undistort, scenes=scenes)
         tot = barrier_max(world, float(sum(ms)))
         med, p95 = agreement(fmaps, chosen_maps)
         out["forms"][name] = {"value": world * len(views) * args.attr_steps / (tot / 1000.0),
                               "accuracy": accuracy(fmaps, truths, rng),
                               "vs_chosen_median_rel_depth_diff": med, "vs_chosen_p95_rel_depth_diff": p95}
+        if staging == 2:
+            out["forms"][name]["windows_staged_frac"] = fst.windows_staged / max(fst.windows_evaluated, 1)
+        if name == "batched_fp16_exact_gauss_newton":
+            exact_maps = fmaps
+        elif name == "batched_fp16_exact_gauss_newton_staged_windows":
+            # the schedules read the same texels with the same arithmetic
+            out["forms"][name]["bit_identical_to_texture_reads"] = all(
+                np.array_equal(a.depth, b.depth, equal_nan=True) and np.array_equal(a.cost, b.cost, equal_nan=True)
+                for a, b in zip(fmaps, exact_maps))
     out["forms"]["chosen"] = {"value": chosen_value, "form": "the timed form of this line"}
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -628,7 +644,9 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
     out["note"] = ("plain = FP32 storage, exact interpolation, one launch per view, golden section, every iteration "
                    "at full resolution; each form adds one change: batched, FP16 storage, Gauss-Newton, texture-unit "
                    "interpolation (8-bit weights); chosen adds coarse-to-fine (the first iterations on the "
-                   "half-resolution level, the same total)")
+                   "half-resolution level, the same total).  Beside the chain: the exact Gauss-Newton form with "
+                   "its source windows staged in shared memory by TMA (window_staging = 2; the same maps as its "
+                   "texture reads, bit for bit), alone and with coarse-to-fine")
     return out
 
 
@@ -768,10 +786,10 @@ def run_gpu(args):
     s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
     # FLOP model: per source window sampled K*K*26 + 30, per hypothesis 40
     flop_per_window, flop_per_hyp_setup = K * K * 26 + 30, 40
-    mk = lambda fp16, interp, per_view, refine, coarse=args.coarse: M.Options(
+    mk = lambda fp16, interp, per_view, refine, coarse=args.coarse, staging=args.window_staging: M.Options(
         mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
         refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
-        tile_rows=args.tile_rows, coarse_iterations=coarse)
+        tile_rows=args.tile_rows, coarse_iterations=coarse, window_staging=staging if interp == 0 else 0)
     opts = mk(args.fp16, args.interp, args.per_view, args.refine)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -1285,6 +1303,8 @@ def main():
     ap.add_argument("--prefilter", action="store_true", help="3x3 binomial pre-filter at staging")
     ap.add_argument("--sampling", type=int, default=0, help="0 pixel-centre windows, 1 the reference's convention")
     ap.add_argument("--interp", type=int, default=None, help="0 exact FP32 bilinear, 1 texture-unit bilinear")
+    ap.add_argument("--window-staging", type=int, default=0, choices=[0, 1, 2],
+                    help="exact interpolation: 0 autotuned, 1 texture reads, 2 source windows staged in shared memory")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--full-map", action="store_true",

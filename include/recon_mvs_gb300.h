@@ -164,6 +164,13 @@ typedef struct recon_mvs_options {
                                 the staged images, focal lengths and principal point halved), and the
                                 full-resolution search starts from the planes they found: coarse-to-fine
                                 initialisation, the configured iteration count in total */
+  int32_t window_staging;    /* plane mode sweep, exact interpolation with FP32 or FP16 storage, 7x7 or
+                                11x11 windows: 0 = the autotuner picks the window schedule; 1 = every
+                                source sample read by the texture unit (2x2 gather); 2 = staged: per
+                                candidate and source view each warp copies the source box its windows
+                                cover (up to 40 x 24 texel pairs) into shared memory by TMA and
+                                samples it there, windows whose box does not fit read the texture.  The
+                                maps are the same bit for bit in every schedule */
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list
@@ -229,9 +236,10 @@ typedef struct recon_mvs_stats {
   int32_t ctas_per_sm;           /* its persistent blocks per SM */
   int32_t graph_launches;        /* CUDA-graph replays so far */
   int32_t tune_trials;           /* autotuner searches run by this context */
-  int32_t reserved[1];
+  int32_t window_staging;        /* the sweep's window schedule in the last plane run: 1 = staged boxes */
   uint64_t windows_evaluated;    /* plane sweeps: source windows sampled (a hypothesis samples up to one
                                     per source; views that cannot change its fate are skipped) */
+  uint64_t windows_staged;       /* of them, windows read from a staged shared-memory box */
 } recon_mvs_stats;
 
 /* ---- version and configuration ---------------------------------------- */

@@ -4,7 +4,11 @@ Each .cu translation unit is compiled in parallel, then linked with a static
 CUDA runtime into recon-scanner_gb300/librecon_mvs_gb300.so.  Host code is
 compiled with -ffp-contract=off: a few host-side FP64 compositions feed
 kernels whose outputs are compared bit-exactly with the CPU oracle, on x86
-and on aarch64 (where gcc would otherwise fuse multiply-adds).
+and on aarch64 (where gcc would otherwise fuse multiply-adds).  Device code
+is compiled with -fmad=false: a multiply-add is fused only where the source
+says fmaf, so the same expression rounds the same way wherever it is inlined
+-- the sweep's window schedules, tile shapes and batch forms give the same
+maps bit for bit by construction, not by the compiler's choice at each site.
 """
 from __future__ import annotations
 
@@ -32,7 +36,8 @@ def nvcc() -> str:
 
 
 def _flags(extra=()):
-    return [ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+    return [ARCH, "-O3", "-std=c++17", "-lineinfo", "-fmad=false",
+            "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
             "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, *extra]
 
 

@@ -133,26 +133,26 @@ __device__ __forceinline__ bool adj_sample(const Job& J, const SrcView& S, const
   const int rx = h.x + dx, ry = h.y + dy;
   if (rx < 0 || ry < 0 || rx > J.w - 1 || ry > J.h - 1) return false;
   const float dq0 = (float)dx * h.irfx, dq1 = (float)dy * h.irfy;
-  const float ndq = h.n[0] * dq0 + h.n[1] * dq1;
+  const float ndq = fmaf(h.n[0], dq0, h.n[1] * dq1);
   const float m = h.kappa + ndq;
   if (!(m < 0.0f)) return false;
   // X_k - X_c = d (kappa dq - (n . dq) q_c) / m_k   (exact small quantities)
   const float sc = h.d * rcp_approx(m);
-  const float dX[3] = {sc * (h.kappa * dq0 - ndq * h.qc[0]), sc * (h.kappa * dq1 - ndq * h.qc[1]), -sc * ndq};
+  const float dX[3] = {sc * fmaf(h.kappa, dq0, -ndq * h.qc[0]), sc * fmaf(h.kappa, dq1, -ndq * h.qc[1]), -sc * ndq};
   float dY[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) dY[i] = fmaf(geo.A[i * 3], dX[0], fmaf(geo.A[i * 3 + 1], dX[1], geo.A[i * 3 + 2] * dX[2]));
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     Y[i] = geo.Yc[i] + dY[i];
-    X[i] = h.d * h.qc[i] + dX[i];
+    X[i] = fmaf(h.d, h.qc[i], dX[i]);
   }
   if (!(Y[2] > 1e-9f)) return false;
   const float iz = rcp_approx(Y[2]);
   const float izc = geo.izc;
   // offset from the centre in index coordinates
-  const float du = S.fx * (dY[0] * geo.Yc[2] - geo.Yc[0] * dY[2]) * (iz * izc);
-  const float dv = S.fy * (dY[1] * geo.Yc[2] - geo.Yc[1] * dY[2]) * (iz * izc);
+  const float du = S.fx * fmaf(dY[0], geo.Yc[2], -geo.Yc[0] * dY[2]) * (iz * izc);
+  const float dv = S.fy * fmaf(dY[1], geo.Yc[2], -geo.Yc[1] * dY[2]) * (iz * izc);
   const float tu = geo.fu + du, tv = geo.fv + dv;
   const float fl_u = floorf(tu), fl_v = floorf(tv);
   const float bu = (float)geo.iu + fl_u, bv = (float)geo.iv + fl_v;  // texel indices (exact integers)
@@ -176,7 +176,7 @@ __device__ __forceinline__ bool adj_sample(const Job& J, const SrcView& S, const
     const float a = gu * S.fx * iz, c = gv * S.fy * iz;
     G[0] = a;
     G[1] = c;
-    G[2] = -(a * un + c * vn);
+    G[2] = -fmaf(a, un, c * vn);
   }
   return true;
 }
@@ -259,18 +259,18 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
       // w = A^T G = dI/dX
       float w[3];
 #pragma unroll
-      for (int j = 0; j < 3; ++j) w[j] = A[j] * G[0] + A[3 + j] * G[1] + A[6 + j] * G[2];
+      for (int j = 0; j < 3; ++j) w[j] = fmaf(A[j], G[0], fmaf(A[3 + j], G[1], A[6 + j] * G[2]));
       const float qx = q[0], qy = q[1];  // the sample's ray (z = 1)
-      const float wq = w[0] * qx + w[1] * qy + w[2];
-      const float dd = (w[0] * X[0] + w[1] * X[1] + w[2] * X[2]) * h.id;
+      const float wq = fmaf(w[0], qx, fmaf(w[1], qy, w[2]));
+      const float dd = fmaf(w[0], X[0], fmaf(w[1], X[1], w[2] * X[2])) * h.id;
       const float im = rcp_approx(m);
       const float cn = wq * h.d * (im * im);
       float dn[3];
-      dn[0] = cn * (h.qc[0] * m - h.kappa * qx);
-      dn[1] = cn * (h.qc[1] * m - h.kappa * qy);
-      dn[2] = cn * (h.qc[2] * m - h.kappa);
-      const float dk[3] = {dd, dn[0] * h.nt[0] + dn[1] * h.nt[1] + dn[2] * h.nt[2],
-                           dn[0] * h.np[0] + dn[1] * h.np[1] + dn[2] * h.np[2]};
+      dn[0] = cn * fmaf(h.qc[0], m, -h.kappa * qx);
+      dn[1] = cn * fmaf(h.qc[1], m, -h.kappa * qy);
+      dn[2] = cn * fmaf(h.qc[2], m, -h.kappa);
+      const float dk[3] = {dd, fmaf(dn[0], h.nt[0], fmaf(dn[1], h.nt[1], dn[2] * h.nt[2])),
+                           fmaf(dn[0], h.np[0], fmaf(dn[1], h.np[1], dn[2] * h.np[2]))};
       int t = 0;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -282,8 +282,8 @@ __device__ void view_adjoint(const Job& J, const SrcView& S, const ViewGeo& geo,
       }
       if (kPose) {
         // dI/dw = Y x G, dI/dtau = G
-        const float pk[6] = {Y[1] * G[2] - Y[2] * G[1], Y[2] * G[0] - Y[0] * G[2], Y[0] * G[1] - Y[1] * G[0],
-                             G[0], G[1], G[2]};
+        const float pk[6] = {fmaf(Y[1], G[2], -Y[2] * G[1]), fmaf(Y[2], G[0], -Y[0] * G[2]),
+                             fmaf(Y[0], G[1], -Y[1] * G[0]), G[0], G[1], G[2]};
         int u = 0;
 #pragma unroll
         for (int i = 0; i < 6; ++i) {

@@ -151,7 +151,20 @@ struct SrcView {
   double A[9];
   double bd[3];
   ff Aff[9];  // A in float-float (per-pixel source rays without FP64)
+  // optional: a 2-D TMA map (global memory) over the texel-pair image of this
+  // view -- element (x, y) = {T(x, y), T(x + 1, y)} as two FP32 words, T the
+  // texels the gather object returns -- read in boxes of kStageW x kStageH
+  // elements by the staged-window sweep; null when not built
+  const void* pair_map;
 };
+
+// The source box one warp of the staged-window sweep holds in shared memory:
+// kStageW texel pairs (8 bytes each, an even count: 16-byte TMA rows) x
+// kStageH rows.  A warp's 32 pixels span 16 columns x 4 rows; with an 11 x 11
+// window their footprint at unit scale is 27 x 15 texels, and the box leaves
+// room for the spread of their hypotheses.
+constexpr int kStageW = 40, kStageH = 24;
+constexpr int kStageBytes = kStageW * kStageH * 8;
 
 // Columns of one reference-tile plane staged by a sweep block: the tile's 32
 // same-colour column pairs, 8 margin on the left and 16 on the right (a TMA

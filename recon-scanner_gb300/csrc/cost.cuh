@@ -327,15 +327,66 @@ struct TileRef {
   }
 };
 
+// How the exact fast path reads a sample's 2x2 footprint.  The argument is
+// the footprint's top-left texel relative to the window centre's texel
+// (iu, iv), as the floats mu, mv = n + kM (kM = 1.5 * 2^23, so that the
+// integer n sits in the low mantissa bits).  Both return the footprint in
+// gather order: (x0,y1) (x1,y1) (x1,y0) (x0,y0).
+constexpr float kMagic = 12582912.0f;
+constexpr unsigned kMagicBits = 0x4B400000u;  // __float_as_uint(kMagic)
+
+template <int kMode>
+struct TexGather {  // one 2x2 gather from the source texture
+  cudaTextureObject_t tex;
+  float gxo, gyo;  // (iu + 1) - kM, (iv + 1) - kM: the gather coordinates are exact integers
+  __device__ __forceinline__ float4 operator()(float mu, float mv) const {
+    return gather4<kMode>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo));
+  }
+};
+
+template <int kMode>
+__device__ __forceinline__ TexGather<kMode> tex_gather(cudaTextureObject_t tex, int iu, int iv) {
+  return TexGather<kMode>{tex, ((float)iu + 1.0f) - kMagic, ((float)iv + 1.0f) - kMagic};
+}
+
+// Two 8-byte loads of texel pairs from a warp's staged box (kStageH rows of
+// kStageW pairs {T(x), T(x + 1)}, top-left texel (ax, ay)): the same four
+// texels as the gather.  The element index is clamped into the box, so no
+// read can leave it whatever the coordinates.
+struct BoxFetch {
+  const float2* box;
+  unsigned base;  // element of the centre texel (iu, iv), less kMagicBits * (kStageW + 1)
+  __device__ __forceinline__ float4 operator()(float mu, float mv) const {
+    unsigned i = __float_as_uint(mv) * (unsigned)kStageW + __float_as_uint(mu) + base;
+    i = min(i, (unsigned)(kStageW * (kStageH - 1) - 1));
+    const float2 t = box[i], b = box[i + kStageW];
+    return make_float4(b.x, b.y, t.y, t.x);
+  }
+};
+
+__device__ __forceinline__ BoxFetch box_fetch(const float2* box, int ax, int ay, int iu, int iv) {
+  return BoxFetch{box, (unsigned)((iv - ay) * kStageW + (iu - ax)) - kMagicBits * (unsigned)(kStageW + 1)};
+}
+
+// The bilinear value at fraction (fx, fy) of the footprint whose top-left
+// texel is the window centre's own: bilinear()'s arithmetic on a fetch.
+template <class Fetch>
+__device__ __forceinline__ float centre_sample(const Fetch& f, float fx, float fy) {
+  const float4 g = f(kMagic, kMagic);
+  const float top = fmaf(fx, g.z - g.w, g.w);
+  const float bot = fmaf(fx, g.y - g.x, g.x);
+  return fmaf(fy, bot - top, top);
+}
+
 // One window row of the fast path, fully unrolled.  Floors by magic-number
 // rounding (FMA pipe): m = t' + 1.5*2^23 rounds t' = t - 0.5 to the nearest
 // integer, i.e. floor(t); at exact ties the footprint shifts by one texel
 // with weight 1, which reads the same value (bilinear is continuous).
-template <int H, int kMode, class Row>
-__device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Row& row,
+template <int H, int kMode, class Row, class Fetch>
+__device__ __forceinline__ void plane_row(const Fetch& fetch, cudaTextureObject_t tex_lin, const Row& row,
                                           float& den, float& nu, float& nv, float c0, float A0, float B0, float fum,
-                                          float fvm, float gxo, float gyo, float cuo, float cvo, float rmean, float sc,
-                                          float& r_s, float& r_ss, float& r_rs) {
+                                          float fvm, float cuo, float cvo, float rmean, float sc, float& r_s,
+                                          float& r_ss, float& r_rs) {
   constexpr float kM = 12582912.0f;
 #pragma unroll
   for (int k = 0; k <= 2 * H; ++k) {
@@ -351,7 +402,7 @@ __device__ __forceinline__ void plane_row(cudaTextureObject_t tex, cudaTextureOb
       const float flu = __fsub_rn(mu, kM), flv = __fsub_rn(mv, kM);
       const float wu = __fadd_rn(__fsub_rn(tmu, flu), 0.5f);
       const float wv = __fadd_rn(__fsub_rn(tmv, flv), 0.5f);
-      const float4 g = gather4<kMode>(tex, __fadd_rn(mu, gxo), __fadd_rn(mv, gyo));
+      const float4 g = fetch(mu, mv);
       const float top = fmaf(wu, g.z - g.w, g.w);
       const float bot = fmaf(wu, g.y - g.x, g.x);
       sv = fmaf(wv, bot - top, top) - sc;
@@ -432,13 +483,11 @@ __device__ __forceinline__ void plane_window_masked(const SrcView& S, const Ref&
 
 // The moments of a full window: each row's partial sums in plain FP32 (11
 // terms), the rows combined with Kahan-compensated sums.
-template <int H, int kMode, class Ref>
-__device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaTextureObject_t tex_lin, const Ref& ref,
+template <int H, int kMode, class Ref, class Fetch>
+__device__ __forceinline__ void plane_window_fast(const Fetch& fetch, cudaTextureObject_t tex_lin, const Ref& ref,
                                                   int iu, int iv, float fu, float fv, float A0, float A1, float B0,
                                                   float B1, float c0, float c1, float rmean, float sc, float* acc) {
-  constexpr float kM = 12582912.0f;
   const float fum = fu - 0.5f, fvm = fv - 0.5f;
-  const float gxo = ((float)iu + 1.0f) - kM, gyo = ((float)iv + 1.0f) - kM;
   const float cuo = ((float)iu + 0.5f) + fu, cvo = ((float)iv + 0.5f) + fv;
   float ss = 0.f, sss = 0.f, srs = 0.f;
   float cs = 0.f, css = 0.f, crs = 0.f;
@@ -449,8 +498,8 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
     float nu = fmaf(fdy, A1, -(float)H * A0);
     float nv = fmaf(fdy, B1, -(float)H * B0);
     float r_s = 0.f, r_ss = 0.f, r_rs = 0.f;
-    plane_row<H, kMode>(tex, tex_lin, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, gxo, gyo, cuo,
-                        cvo, rmean, sc, r_s, r_ss, r_rs);
+    plane_row<H, kMode>(fetch, tex_lin, ref.template row<H>(dy), den, nu, nv, c0, A0, B0, fum, fvm, cuo, cvo, rmean,
+                        sc, r_s, r_ss, r_rs);
     kahan_add(ss, cs, r_s);
     kahan_add(sss, css, r_ss);
     kahan_add(srs, crs, r_rs);
@@ -460,12 +509,10 @@ __device__ __forceinline__ void plane_window_fast(cudaTextureObject_t tex, cudaT
   acc[4] = srs;
 }
 
-// H > 0: windows of 2H+1 known at compile time, reference samples through
-// `ref` on the fast path; H == 0: any window size (runtime loop).
-// The window's moments as the adjoint wants them (`mom`, optional): n, the
-// means of the reference and source values, and the centred sums of squares
-// and products -- from sums shifted by (rmean, sc): mean = shift + S / n,
-// centred = S2 - S S' / n.
+// The window's moments as the adjoint wants them: n, the means of the
+// reference and source values, and the centred sums of squares and products
+// -- from sums shifted by (rmean, sc): mean = shift + S / n, centred =
+// S2 - S S' / n.
 __device__ __forceinline__ void window_moments(float* mom, float n, float rmean, float sc, float sr, float srr,
                                                float ss, float sss, float srs) {
   const float inv_n = 1.0f / n;
@@ -477,15 +524,32 @@ __device__ __forceinline__ void window_moments(float* mom, float n, float rmean,
   mom[5] = srs - sr * ss * inv_n;
 }
 
-template <int H, int kMode, class Ref>
-__device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
-                                                      const PlaneHyp& hp, const RefWindow& rw, const Ref& ref,
-                                                      float* mom = nullptr) {
-  ViewResult bad{0.0f, -1};  // nothing sampled
+// Where a plane hypothesis' window falls in one source: the per-sample
+// offsets from the window centre, du = (dx A0 + dy A1) / (1 + dx c0 + dy c1)
+// (dv likewise with B), the centre's texel (iu, iv) and fraction (fu, fv) in
+// the pixel-centre convention (index coordinate = coordinate - 0.5), and the
+// four corners' index coordinates relative to (iu, iv).
+struct WindowPlace {
+  float A0, A1, B0, B1, c0, c1;
+  int iu, iv;
+  float fu, fv;
+  float umin, umax, vmin, vmax;
+  bool full;     // the whole window inside the source, in front of it, on the camera side of the plane
+  bool front;    // the four corners in front of the source and on the camera side of the plane
+  bool outside;  // in front, and every corner beyond one image edge: no sample is valid
+};
+
+// False when the window centre is not in front of the source (nothing is
+// sampled).  The four corners decide the window: all inside (and in front of
+// the source, on the camera side of the plane) -> every sample is valid, by
+// convexity of the projective image of the window; all beyond one image edge
+// -> no sample is valid and the view is invalid without sampling.
+template <int H>
+__device__ __forceinline__ bool place_window(const Job& J, const SrcView& S, const ff P[3], const PlaneHyp& hp,
+                                              const RefWindow& rw, WindowPlace* g) {
   ff u0, v0;
   float xz, mx, my;
-  if (!source_centre(S, P, ff_make(hp.rho), hp.rho, &u0, &v0, &xz, &mx, &my)) return bad;
-  // per-sample offsets from the centre: du = (dx A0 + dy A1) / (1 + dx c0 + dy c1)
+  if (!source_centre(S, P, ff_make(hp.rho), hp.rho, &u0, &v0, &xz, &mx, &my)) return false;
   const float G0x = fmaf(hp.s0, S.b[0], S.Ac0[0]);
   const float G0y = fmaf(hp.s0, S.b[1], S.Ac0[1]);
   const float G0z = fmaf(hp.s0, S.b[2], S.Ac0[2]);
@@ -493,35 +557,26 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
   const float G1y = fmaf(hp.s1, S.b[1], S.Ac1[1]);
   const float G1z = fmaf(hp.s1, S.b[2], S.Ac1[2]);
   const float iz = rcp_approx(xz);
-  const float A0 = S.fx * (G0x - mx * G0z) * iz;
-  const float A1 = S.fx * (G1x - mx * G1z) * iz;
-  const float B0 = S.fy * (G0y - my * G0z) * iz;
-  const float B1 = S.fy * (G1y - my * G1z) * iz;
-  const float c0 = G0z * iz;
-  const float c1 = G1z * iz;
-  // pixel-centre convention: index coordinate = coordinate - 0.5
-  int iu, iv;
-  float fu, fv;
+  g->A0 = S.fx * (G0x - mx * G0z) * iz;
+  g->A1 = S.fx * (G1x - mx * G1z) * iz;
+  g->B0 = S.fy * (G0y - my * G0z) * iz;
+  g->B1 = S.fy * (G1y - my * G1z) * iz;
+  g->c0 = G0z * iz;
+  g->c1 = G1z * iz;
   const float shift = J.half_pixel ? 0.0f : -0.5f;
-  ff_floor_frac(ff_add(u0, ff_make(shift)), &iu, &fu);
-  ff_floor_frac(ff_add(v0, ff_make(shift)), &iv, &fv);
+  ff_floor_frac(ff_add(u0, ff_make(shift)), &g->iu, &g->fu);
+  ff_floor_frac(ff_add(v0, ff_make(shift)), &g->iv, &g->fv);
   const int h = H > 0 ? H : J.patch_half;
   const float fh = (float)h;
-  // fast path: the four corners (hence, by convexity, the whole window)
-  // inside the source, in front of it, and on the camera side of the plane
-  // The four corners decide the window: all inside (and in front of the
-  // source, on the camera side of the plane) -> every sample is valid, by
-  // convexity of the projective image of the window; all beyond one image
-  // edge -> no sample is valid and the view is invalid without sampling.
-  bool full = rw.full, front = true;
+  bool front = true;
   float umin_c = 3.4e38f, umax_c = -3.4e38f, vmin_c = 3.4e38f, vmax_c = -3.4e38f;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const float dx = (c & 1) ? fh : -fh, dy = (c & 2) ? fh : -fh;
-    const float den = fmaf(dx, c0, fmaf(dy, c1, 1.0f));
+    const float den = fmaf(dx, g->c0, fmaf(dy, g->c1, 1.0f));
     const float rd = rcp_approx(den);
-    const float tu = fu + fmaf(dx, A0, dy * A1) * rd;
-    const float tv = fv + fmaf(dx, B0, dy * B1) * rd;
+    const float tu = g->fu + fmaf(dx, g->A0, dy * g->A1) * rd;
+    const float tv = g->fv + fmaf(dx, g->B0, dy * g->B1) * rd;
     const float nr = hp.kappa + dx * hp.ex + dy * hp.ey;
     front = front && den > 0.0f && nr < 0.0f;
     umin_c = fminf(umin_c, tu);
@@ -529,38 +584,90 @@ __device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcVie
     vmin_c = fminf(vmin_c, tv);
     vmax_c = fmaxf(vmax_c, tv);
   }
-  const float ulo = (float)(-iu), uhi = (float)(S.w - 1 - iu), vlo = (float)(-iv), vhi = (float)(S.h - 1 - iv);
-  full = full && front && umin_c >= ulo + 0.001f && umax_c <= uhi - 0.001f && vmin_c >= vlo + 0.001f &&
-         vmax_c <= vhi - 0.001f;
-  const bool outside = front && (umax_c < ulo - 0.001f || umin_c > uhi + 0.001f || vmax_c < vlo - 0.001f ||
-                                 vmin_c > vhi + 0.001f);
+  const float ulo = (float)(-g->iu), uhi = (float)(S.w - 1 - g->iu), vlo = (float)(-g->iv),
+              vhi = (float)(S.h - 1 - g->iv);
+  g->front = front;
+  g->full = rw.full && front && umin_c >= ulo + 0.001f && umax_c <= uhi - 0.001f && vmin_c >= vlo + 0.001f &&
+            vmax_c <= vhi - 0.001f;
+  g->outside = front && (umax_c < ulo - 0.001f || umin_c > uhi + 0.001f || vmax_c < vlo - 0.001f ||
+                         vmin_c > vhi + 0.001f);
+  g->umin = umin_c;
+  g->umax = umax_c;
+  g->vmin = vmin_c;
+  g->vmax = vmax_c;
+  return true;
+}
+
+// The NCC of a window placed by place_window, its samples read from the
+// source texture.
+template <int H, int kMode, class Ref>
+__device__ __forceinline__ ViewResult eval_view_placed(const Job& J, const SrcView& S, int x, int y, const WindowPlace& g,
+                                                    const PlaneHyp& hp, const RefWindow& rw, const Ref& ref,
+                                                    float* mom = nullptr) {
+  ViewResult bad{0.0f, -1};  // nothing sampled
+  const int iu = g.iu, iv = g.iv;
+  const float fu = g.fu, fv = g.fv;
   // source centring value: the sample at the window centre (clamped read)
   const float sc = kMode == kSrcTex ? tex2D<float>(S.tex_lin, (float)iu + 0.5f + fu, (float)iv + 0.5f + fv)
                                     : bilinear<kMode>(S.tex, (float)iu, (float)iv, fu, fv);
   float acc[5], n;
+  const int h = H > 0 ? H : J.patch_half;
   const int K = 2 * h + 1;
   const int min_valid = J.min_valid;
-  if (outside) return bad;
+  if (g.outside) return bad;
   if constexpr (H > 0) {
-    if (full) {
-      plane_window_fast<H, kMode>(S.tex, S.tex_lin, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc);
+    if (g.full) {
+      plane_window_fast<H, kMode>(tex_gather<kMode>(S.tex, iu, iv), S.tex_lin, ref, iu, iv, fu, fv, g.A0, g.A1, g.B0,
+                                  g.B1, g.c0, g.c1, rw.mean, sc, acc);
       if (mom) window_moments(mom, (float)(K * K), rw.mean, sc, 0.0f, rw.sxx, acc[2], acc[3], acc[4]);
       return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
     }
-    if (rw.full && front) {
+    if (rw.full && g.front) {
       // straddles a source border: masked samples, reference from the tile
-      plane_window_masked<H, kMode>(S, ref, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, rw.mean, sc, acc, &n);
+      plane_window_masked<H, kMode>(S, ref, iu, iv, fu, fv, g.A0, g.A1, g.B0, g.B1, g.c0, g.c1, rw.mean, sc, acc,
+                                    &n);
       if (mom && n > 0.f) window_moments(mom, n, rw.mean, sc, acc[0], acc[1], acc[2], acc[3], acc[4]);
       return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
     }
-  } else if (full) {
-    plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  } else if (g.full) {
+    plane_window<true, kMode>(J, S, x, y, iu, iv, fu, fv, g.A0, g.A1, g.B0, g.B1, g.c0, g.c1, hp, rw.mean, sc, acc,
+                              &n);
     if (mom) window_moments(mom, (float)(K * K), rw.mean, sc, 0.0f, rw.sxx, acc[2], acc[3], acc[4]);
     return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], min_valid);
   }
-  plane_window<false, kMode>(J, S, x, y, iu, iv, fu, fv, A0, A1, B0, B1, c0, c1, hp, rw.mean, sc, acc, &n);
+  plane_window<false, kMode>(J, S, x, y, iu, iv, fu, fv, g.A0, g.A1, g.B0, g.B1, g.c0, g.c1, hp, rw.mean, sc, acc,
+                             &n);
   if (mom && n > 0.f) window_moments(mom, n, rw.mean, sc, acc[0], acc[1], acc[2], acc[3], acc[4]);
   return ncc_from_moments(n, acc[0], acc[1], acc[2], acc[3], acc[4], min_valid);
+}
+
+// The NCC of one hypothesis against one source view.  H > 0: windows of
+// 2H+1 known at compile time, reference samples through `ref` on the fast
+// path; H == 0: any window size (runtime loop).  The window's moments as the
+// adjoint wants them (`mom`, optional): n, the means of the reference and
+// source values, and the centred sums of squares and products.
+template <int H, int kMode, class Ref>
+__device__ __forceinline__ ViewResult eval_view_plane(const Job& J, const SrcView& S, int x, int y, const ff P[3],
+                                                      const PlaneHyp& hp, const RefWindow& rw, const Ref& ref,
+                                                      float* mom = nullptr) {
+  WindowPlace g;
+  if (!place_window<H>(J, S, P, hp, rw, &g)) return ViewResult{0.0f, -1};
+  return eval_view_placed<H, kMode>(J, S, x, y, g, hp, rw, ref, mom);
+}
+
+// The NCC of a full window (place_window's `full`) whose samples are read
+// from a warp's staged box: the fast path's arithmetic, footprints from the
+// box instead of the texture -- the same value as eval_view_placed, bit for bit.
+template <int H, class Ref>
+__device__ __forceinline__ ViewResult eval_view_box(const Job& J, const WindowPlace& g, const RefWindow& rw, const Ref& ref,
+                                                    const float2* box, int ax, int ay) {
+  const BoxFetch f = box_fetch(box, ax, ay, g.iu, g.iv);
+  const float sc = centre_sample(f, g.fu, g.fv);
+  float acc[5];
+  constexpr int K = 2 * H + 1;
+  plane_window_fast<H, kSrcExact>(f, 0, ref, g.iu, g.iv, g.fu, g.fv, g.A0, g.A1, g.B0, g.B1, g.c0, g.c1, rw.mean, sc,
+                                  acc);
+  return ncc_from_moments((float)(K * K), 0.0f, rw.sxx, acc[2], acc[3], acc[4], J.min_valid);
 }
 
 // Reference-window statistics for a pixel: mean and centred sum of squares of

@@ -183,6 +183,10 @@ struct StagedImage {
   DevArray<float> f32;
   bool is_f32 = false;
   std::unique_ptr<Texture> tex;
+  // the texel-pair image of `tex` and its TMA map (the staged-window
+  // schedule's source), built on first use
+  DevArray<float2> pair;
+  DevArray<CUtensorMap> pair_map;
   DevArray<float> ref, box, de;
   int de_pitch = 0;  // floats per row of `de` (a multiple of 4: 16-byte rows for TMA)
   bool has_ref = false;
@@ -233,14 +237,16 @@ static int row_choice_index(int rows) {
 struct TuneKey {
   int device, patch_half, hw, storage, max_src, njobs;
   long long pixels;
+  int staging;  // the schedules searched: 0 both, 1 texture reads only, 2 staged boxes only
   bool operator<(const TuneKey& o) const {
-    return std::tie(device, patch_half, hw, storage, max_src, njobs, pixels) <
-           std::tie(o.device, o.patch_half, o.hw, o.storage, o.max_src, o.njobs, o.pixels);
+    return std::tie(device, patch_half, hw, storage, max_src, njobs, pixels, staging) <
+           std::tie(o.device, o.patch_half, o.hw, o.storage, o.max_src, o.njobs, o.pixels, o.staging);
   }
 };
 struct TuneChoice {
   int rows = 4;
   int ctas_per_sm = 0;
+  int staged = 0;
 };
 static std::mutex g_tune_mu;
 static std::map<TuneKey, TuneChoice>& tune_cache() {
@@ -262,6 +268,8 @@ struct PlaneGroup {
   DevArray<int> queues;     // one work counter per half-sweep
   DevArray<CUtensorMap> tmaps[kNumRowChoices];  // per row choice, one per job (windows with H > 0)
   int rows = 4, ctas_per_sm = 1, grid = 1;
+  bool can_stage = false;  // exact reads, 7x7 or 11x11, every source with a pair map
+  int staged = 0;          // the sweep's window schedule: 1 = staged boxes
 
   int nj() const { return (int)jobs.size(); }
   const PlaneBatch& sweep_batch(int rows_) const { return *sweep[row_choice_index(rows_)]; }
@@ -318,6 +326,13 @@ struct Context {
       fail(RECON_ERR_INVALID_ARGUMENT, "U8 storage needs plane mode");
     if (o.storage == RECON_MVS_STORAGE_BF16 && (o.mode != RECON_MVS_MODE_PLANE || o.interp != 0))
       fail(RECON_ERR_INVALID_ARGUMENT, "BF16 storage needs plane mode with exact interpolation (interp = 0)");
+    if (o.window_staging < 0 || o.window_staging > 2)
+      fail(RECON_ERR_INVALID_ARGUMENT, "window_staging must be 0 (autotuned), 1 (off) or 2 (on)");
+    if (o.window_staging == 2 &&
+        (o.mode != RECON_MVS_MODE_PLANE || o.interp != 0 ||
+         (o.storage != RECON_MVS_STORAGE_FP32 && o.storage != RECON_MVS_STORAGE_FP16)))
+      fail(RECON_ERR_INVALID_ARGUMENT,
+           "window_staging = 2 needs plane mode, exact interpolation and FP32 or FP16 storage");
     device = o.device;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -327,8 +342,8 @@ struct Context {
     CK(cudaEventCreate(&ev_sweep0));
     CK(cudaEventCreate(&ev_sweep1));
     CK(cudaEventCreate(&ev_end));
-    counter.alloc(2);  // hypotheses, source windows sampled
-    CK(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned long long), stream));
+    counter.alloc(3);  // hypotheses, source windows sampled, of them read from staged boxes
+    CK(cudaMemsetAsync(counter.p, 0, 3 * sizeof(unsigned long long), stream));
     err.alloc(1);
     CK(cudaMemsetAsync(err.p, 0, sizeof(int), stream));
   }
@@ -565,6 +580,49 @@ static void ensure_texture(Context& C, StagedImage& I) {
   CK(cudaStreamSynchronize(C.stream));  // the context's staging buffer is reused
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn) fail(RECON_ERR_MVS_GPU_FAILURE, "cuTensorMapEncodeTiled unavailable");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  return encode;
+}
+
+// Sources get pair images when the staged-window schedule can apply: plane
+// mode, exact interpolation, FP32 or FP16 storage, staging not switched off.
+static bool wants_pairs(const Context& C) {
+  return C.opts.mode == RECON_MVS_MODE_PLANE && C.opts.interp == 0 && C.opts.window_staging != 1 &&
+         (C.opts.storage == RECON_MVS_STORAGE_FP32 || C.opts.storage == RECON_MVS_STORAGE_FP16);
+}
+
+// The texel-pair image of a staged image's texture -- {T(x, y), T(x + 1, y)}
+// as two FP32 words, rows padded to an even count (16-byte pitch) -- and its
+// 2-D TMA map of 8-byte elements, read in kStageW x kStageH boxes (zeros
+// outside the image).
+static void ensure_pair(Context& C, StagedImage& I) {
+  if (I.pair_map.p) return;
+  ensure_texture(C, I);
+  const int pitch = (I.w + 1) & ~1;
+  I.pair.alloc((size_t)pitch * I.h);
+  CK(launch_pair_image(I.tex->tex, I.w, I.h, I.pair.p, pitch, C.stream));
+  const cuuint64_t dims[2] = {(cuuint64_t)I.w, (cuuint64_t)I.h};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)kStageW, (cuuint32_t)kStageH};
+  const cuuint32_t estr[2] = {1, 1};
+  CUtensorMap map;
+  const CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, I.pair.p, dims, strides, box, estr,
+                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(RECON_ERR_MVS_GPU_FAILURE, "cuTensorMapEncodeTiled failed (pair image)");
+  I.pair_map.alloc(1);
+  CK(cudaMemcpyAsync(I.pair_map.p, &map, sizeof(map), cudaMemcpyHostToDevice, C.stream));
+  CK(cudaStreamSynchronize(C.stream));  // `map` lives on this stack frame
+}
+
 static void ensure_reference(Context& C, StagedImage& I) {
   if (I.has_ref) return;
   const bool plane = C.opts.mode == RECON_MVS_MODE_PLANE;
@@ -676,6 +734,10 @@ static std::unique_ptr<JobData> build_job_data(Context& C, const std::shared_ptr
     std::memset(&S, 0, sizeof(S));
     S.tex = I.tex->tex;
     S.tex_lin = I.tex->tex_lin;
+    if (plane && wants_pairs(C) && (cfg->patch_size / 2 == 5 || cfg->patch_size / 2 == 3)) {
+      ensure_pair(C, I);
+      S.pair_map = I.pair_map.p;
+    }
     S.w = I.w;
     S.h = I.h;
     S.fx = (float)sk.fx;
@@ -885,13 +947,7 @@ static JobData& get_job(Context& C, int id) {
 // FP32 with 16-byte row pitch, read in boxes of kTileCols columns x box_rows
 // rows x both planes (what one sweep tile stages), zeros outside.
 static void encode_ref_tile_map(const JobData& D, int box_rows, CUtensorMap* out) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !fn) fail(RECON_ERR_MVS_GPU_FAILURE, "cuTensorMapEncodeTiled unavailable");
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }();
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   const Job& J = D.J;
   const cuuint64_t dims[3] = {(cuuint64_t)J.ref_half_w, (cuuint64_t)J.h, 2};
   const cuuint64_t strides[2] = {(cuuint64_t)J.ref_pitch * sizeof(float),
@@ -952,6 +1008,9 @@ static void build_group(Context& C, PlaneGroup& G) {
     CK(cudaMemcpy(G.tmaps[r].p, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice));
     G.sweep[r]->tmaps = G.tmaps[r].p;
   }
+  G.can_stage = G.mode == kSrcExact && (G.patch_half == 5 || G.patch_half == 3);
+  for (int j = 0; j < n && G.can_stage; ++j)
+    for (const SrcView& S : G.jobs[j]->host_src) G.can_stage = G.can_stage && S.pair_map != nullptr;
   G.active.assign(std::max(G.max_iters, 1), 0);
   for (int it = 0; it < G.max_iters; ++it)
     for (int j = 0; j < n; ++j)
@@ -965,76 +1024,87 @@ static int sm_count(int device) {
   return std::max(n, 1);
 }
 
-// The autotuner: times one half-sweep of the group itself for every tile
-// shape (rows per tile) and every persistent grid (resident blocks per SM,
+// The autotuner: times one half-sweep of the group itself for every window
+// schedule (texture reads, or staged boxes where exact reads allow them),
+// tile shape (rows per tile) and persistent grid (resident blocks per SM,
 // full or one less), starting each trial from a fresh init, and keeps the
 // fastest.  The choice cannot change results -- every pixel computes the same
-// thing whatever the tile -- and is cached per (device, window, interpolation,
-// storage, max sources, job count, pixel count).  Explicit options.tile_rows
-// skips the search.
+// thing whatever the tile or schedule -- and is cached per (device, window,
+// interpolation, storage, max sources, job count, pixel count, staging
+// option).  Explicit options.tile_rows skips the search (and takes staged
+// boxes only when window_staging = 2).
 static void tune_group(Context& C, PlaneGroup& G) {
   const int nsm = sm_count(C.device);
-  auto set_shape = [&](int rows, int ctas) {
+  auto set_shape = [&](int rows, int ctas, int staged) {
     G.rows = rows;
     G.ctas_per_sm = ctas;
     G.grid = ctas * nsm;
+    G.staged = staged;
   };
-  auto occupancy = [&](int rows) {
+  auto occupancy = [&](int rows, int staged) {
     int b = 0;
-    CK(plane_sweep_occupancy(G.patch_half, G.mode, G.max_src, rows, &b));
+    CK(plane_sweep_occupancy(G.patch_half, G.mode, G.max_src, rows, staged, &b));
     return b;
   };
+  // the window schedules to consider: staged boxes only where they apply
+  const int stage_lo = (G.can_stage && C.opts.window_staging == 2) ? 1 : 0;
+  const int stage_hi = (G.can_stage && C.opts.window_staging != 1) ? 1 : 0;
   if (C.opts.tile_rows != 0) {
-    const int b = occupancy(C.opts.tile_rows);
+    const int b = occupancy(C.opts.tile_rows, stage_lo);
     if (b < 1) fail(RECON_ERR_INVALID_ARGUMENT, "tile_rows: the sweep kernel does not fit on an SM");
-    set_shape(C.opts.tile_rows, b);
+    set_shape(C.opts.tile_rows, b, stage_lo);
     return;
   }
-  const TuneKey key{C.device, G.patch_half, G.mode, C.opts.storage, G.max_src, G.nj(), G.pixels};
+  const TuneKey key{C.device, G.patch_half, G.mode, C.opts.storage, G.max_src, G.nj(), G.pixels,
+                    C.opts.window_staging};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = tune_cache().find(key);
     if (it != tune_cache().end()) {
-      set_shape(it->second.rows, it->second.ctas_per_sm);
+      set_shape(it->second.rows, it->second.ctas_per_sm, it->second.staged);
       return;
     }
   }
   if (G.max_iters == 0) {
-    set_shape(4, std::max(1, occupancy(4)));
+    set_shape(4, std::max(1, occupancy(4, stage_lo)), stage_lo);
     return;
   }
-  unsigned long long saved[2] = {0, 0};
+  unsigned long long saved[3] = {0, 0, 0};
   CK(cudaMemcpyAsync(saved, C.counter.p, sizeof(saved), cudaMemcpyDeviceToHost, C.stream));
   CK(cudaStreamSynchronize(C.stream));
   float best_ms = 1e30f;
   TuneChoice best;
-  for (int rows : kRowChoices) {
-    const int b = occupancy(rows);
-    for (int ctas = b; ctas >= std::max(1, b - 1); --ctas) {
-      float ms = 0.f;
-      for (int rep = 0; rep < 2; ++rep) {  // the first trial also loads the kernel
-        CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
-        CK(cudaEventRecord(C.ev_sweep0, C.stream));
-        CK(launch_plane_sweep(G.sweep_batch(rows), G.sweep_total(rows, 0), G.queues.p, G.patch_half, G.mode, G.max_src,
-                              rows, ctas * nsm, 0, 0, C.stream));
-        CK(cudaEventRecord(C.ev_sweep1, C.stream));
-        CK(cudaEventSynchronize(C.ev_sweep1));
-        CK(cudaEventElapsedTime(&ms, C.ev_sweep0, C.ev_sweep1));
-      }
-      if (ms < best_ms) {
-        best_ms = ms;
-        best.rows = rows;
-        best.ctas_per_sm = ctas;
+  best.staged = stage_lo;
+  for (int staged = stage_lo; staged <= stage_hi; ++staged)
+    for (int rows : kRowChoices) {
+      const int b = occupancy(rows, staged);
+      for (int ctas = b; ctas >= std::max(1, b - 1); --ctas) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {  // the first trial also loads the kernel
+          CK(launch_plane_init(*G.pix, G.patch_half, G.mode, G.max_src, G.queues.p, (int)G.queues.n, C.stream));
+          CK(cudaEventRecord(C.ev_sweep0, C.stream));
+          CK(launch_plane_sweep(G.sweep_batch(rows), G.sweep_total(rows, 0), G.queues.p, G.patch_half, G.mode,
+                                G.max_src, rows, staged, ctas * nsm, 0, 0, C.stream));
+          CK(cudaEventRecord(C.ev_sweep1, C.stream));
+          CK(cudaEventSynchronize(C.ev_sweep1));
+          CK(cudaEventElapsedTime(&ms, C.ev_sweep0, C.ev_sweep1));
+        }
+        if (ms < best_ms) {
+          best_ms = ms;
+          best.rows = rows;
+          best.ctas_per_sm = ctas;
+          best.staged = staged;
+        }
       }
     }
-  }
+  if (best_ms >= 1e30f) fail(RECON_ERR_MVS_GPU_FAILURE, "the sweep kernel does not fit on an SM");
   CK(cudaMemcpyAsync(C.counter.p, saved, sizeof(saved), cudaMemcpyHostToDevice, C.stream));
   CK(cudaStreamSynchronize(C.stream));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     tune_cache()[key] = best;
   }
-  set_shape(best.rows, best.ctas_per_sm);
+  set_shape(best.rows, best.ctas_per_sm, best.staged);
   C.stats.tune_trials += 1;
 }
 
@@ -1052,7 +1122,7 @@ static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
       for (int it = 0; it < G.max_iters; ++it)
         for (int color = 0; color < 2; ++color)
           CK(launch_plane_sweep(G.sweep_batch(G.rows), G.sweep_total(G.rows, it), G.queues.p + 2 * it + color,
-                                G.patch_half, G.mode, G.max_src, G.rows, G.grid, color, it, C.stream));
+                                G.patch_half, G.mode, G.max_src, G.rows, G.staged, G.grid, color, it, C.stream));
     }
     for (auto& g : P.groups) {
       PlaneGroup& G = *g;
@@ -1065,7 +1135,7 @@ static void enqueue_stage(Context& C, PlanePlan& P, int stage) {
       for (int it = 0; it < G.max_iters; ++it)
         for (int color = 0; color < 2; ++color) {
           CK(launch_plane_sweep(G.sweep_batch(G.rows), G.sweep_total(G.rows, it), G.queues.p + 2 * it + color,
-                                G.patch_half, G.mode, G.max_src, G.rows, G.grid, color, it, C.stream));
+                                G.patch_half, G.mode, G.max_src, G.rows, G.staged, G.grid, color, it, C.stream));
           ++launches;
         }
     }
@@ -1163,6 +1233,7 @@ static void run_plane_jobs(Context& C, const std::vector<JobData*>& jobs, const 
   C.stats.last_sweep_launches = P.sweep_launches;
   C.stats.tile_rows = P.groups[0]->rows;
   C.stats.ctas_per_sm = P.groups[0]->ctas_per_sm;
+  C.stats.window_staging = P.groups[0]->staged;
 }
 
 // ---- compat mode ----------------------------------------------------------
@@ -1327,12 +1398,14 @@ static void check_device_error(Context& C) {
   }
 }
 
-// The evaluation counters (hypotheses, source windows sampled) into the stats.
+// The evaluation counters (hypotheses, source windows sampled, of them read
+// from staged boxes) into the stats.
 static void read_counters(Context& C) {
-  unsigned long long ev[2] = {0, 0};
+  unsigned long long ev[3] = {0, 0, 0};
   CK(cudaMemcpy(ev, C.counter.p, sizeof(ev), cudaMemcpyDeviceToHost));
   C.stats.hypotheses_evaluated = ev[0];
   C.stats.windows_evaluated = ev[1];
+  C.stats.windows_staged = ev[2];
 }
 
 static void finish_stats(Context& C) {

@@ -125,9 +125,18 @@ struct PlaneBatch {
 static_assert(sizeof(PlaneBatch) + 64 <= 32764, "PlaneBatch exceeds the kernel-parameter limit");
 cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int max_src, int* queues, int num_queues,
                               cudaStream_t st);
-cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int* blocks_per_sm);
+// `staged` = 1: the staged-window schedule of the sweep (exact interpolation,
+// 7x7 or 11x11 windows, every source with a pair map): per (candidate, view)
+// a warp copies the source box its windows cover into shared memory by TMA
+// and samples it there; windows whose warp footprint does not fit read the
+// texture.  The maps are the same either way.
+cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int staged, int* blocks_per_sm);
 cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, int mode, int max_src,
-                               int rows, int grid, int color, int iter, cudaStream_t st);
+                               int rows, int staged, int grid, int color, int iter, cudaStream_t st);
+// The texel-pair image of a source texture (the staged-window schedule's
+// TMA source): out[y * pitch + x] = {T(x, y), T(x + 1, y)}, the second word
+// 0 in the last column.
+cudaError_t launch_pair_image(cudaTextureObject_t tex, int w, int h, float2* out, int pitch, cudaStream_t st);
 cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st);
 cudaError_t launch_plane_refine_gn(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st);
 cudaError_t launch_plane_output(const PlaneBatch& B, cudaStream_t st);

@@ -104,26 +104,22 @@ __device__ __forceinline__ HypCost finish_plane(float* best, float sum_all, int 
   return r;
 }
 
-// `beat`: the cost a candidate must get below to be taken (the caller keeps
-// it only if cost < beat).  View costs lie in [0, 2], so after each view the
-// final cost is bounded below by letting every remaining view be valid at
-// cost 0: with K = best_k (or all views), n valid so far, r views left and
-// k' = min(K, n + r), cost >= (sum of the k' - r lowest costs so far) / k'.
-// Once that bound is above `beat` (with a relative margin that covers the
-// rounding of both sums) the remaining views cannot change the decision and
-// are not evaluated: the candidate is returned as rejected.
-template <int H, int kMode, class Ref>
-__device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
-                                  float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
-                                  int* counts = nullptr, float beat = kCostInf) {
-  HypCost bad{kCostInf, 0};
-  PlaneHyp hp;
-  if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max || !make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) {
-    if (view_cost)
-      for (int s = 0; s < J.num_src; ++s) view_cost[s] = kCostInf;
-    return bad;
-  }
-  if (counts) ++counts[0];
+// The cost of one plane hypothesis from its views: view(s, active) evaluates
+// source view s and returns its NCC (valid = -1: not sampled); the cost is
+// the mean of the best_k view costs 1 - NCC.  Exact pruning: view costs lie
+// in [0, 2], so after each view the final cost is bounded below by letting
+// every remaining view be valid at cost 0 -- with K = best_k (or all views),
+// n valid so far, r views left and k' = min(K, n + r), cost >= (sum of the
+// k' - r lowest costs so far) / k'.  Once that bound is above `beat` (the
+// cost a candidate must get below to be taken, with a relative margin that
+// covers the rounding of both sums) the remaining views cannot change the
+// decision and are not evaluated: the candidate is returned as rejected.
+// kCollective: view() is called for every view whatever this lane's state
+// (the staged schedule's views are warp-collective), `active` telling it
+// whether this lane's hypothesis still needs the view.
+template <bool kCollective, class ViewFn>
+__device__ __forceinline__ HypCost plane_hyp_cost(const Job& J, bool live, const ViewFn& view, float* view_cost,
+                                                  int* counts, float beat) {
   float best[kMaxBestK];
 #pragma unroll
   for (int i = 0; i < kMaxBestK; ++i) best[i] = kCostInf;
@@ -135,11 +131,10 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
   bool pruned = false;
   for (int s = 0; s < J.num_src; ++s) {
     ViewResult v{0.0f, -1};  // skipped: not sampled
-    if (!pruned) {
-      ff P[3];
-      pc.get(s, P);
-      v = eval_view_plane<H, kMode>(J, J.src[s], x, y, P, hp, rw, ref);
-    }
+    if (kCollective)
+      v = view(s, live && !pruned);
+    else if (!pruned)
+      v = view(s, true);
     if (counts) counts[1] += v.valid >= 0;
     float c = kCostInf;
     if (v.valid > 0) {
@@ -170,8 +165,30 @@ __device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, 
       pruned = pruned || (j > 0 && lb > bar * (float)kk);
     }
   }
-  if (pruned) return HypCost{kCostInf, 0};
+  if (!live || pruned) return HypCost{kCostInf, 0};
   return finish_plane(best, sum_all, nvalid, J.best_k, J.photo_threshold);
+}
+
+template <int H, int kMode, class Ref>
+__device__ HypCost eval_plane_hyp(const Job& J, const PCache& pc, int x, int y, float rx, float ry, float rho,
+                                  float nx, float ny, float nz, const RefWindow& rw, const Ref& ref, float* view_cost,
+                                  int* counts = nullptr, float beat = kCostInf) {
+  HypCost bad{kCostInf, 0};
+  PlaneHyp hp;
+  if (!(rho > 0.0f) || rho < J.rho_min || rho > J.rho_max || !make_plane_hyp(J, rx, ry, rho, nx, ny, nz, &hp)) {
+    if (view_cost)
+      for (int s = 0; s < J.num_src; ++s) view_cost[s] = kCostInf;
+    return bad;
+  }
+  if (counts) ++counts[0];
+  return plane_hyp_cost<false>(
+      J, true,
+      [&](int s, bool) {
+        ff P[3];
+        pc.get(s, P);
+        return eval_view_plane<H, kMode>(J, J.src[s], x, y, P, hp, rw, ref);
+      },
+      view_cost, counts, beat);
 }
 
 // COMPAT: 1 - mean NCC over valid views (patchmatch_stereo.cpp:344-418).
@@ -435,6 +452,89 @@ __device__ __forceinline__ RefWindow tile_window(const Job& J, const TileRef& t,
   return rw;
 }
 
+// Propagation candidate of region r (0-7) for pixel (x, y): the plane of the
+// region's lowest-cost neighbour, carried to this pixel's ray.  False when the
+// region offers nothing to learn: no neighbour with a finite cost, the
+// current plane again (same normal, inverse depth within rounding of the
+// transfer -- in a converged region most regions propose exactly this), or,
+// with pruning, the previous region's candidate again (the same plane reached
+// through another neighbour: it was rejected, and its cost has not changed).
+__device__ __forceinline__ bool propagation_candidate(const Job& J, int x, int y, int r, float rx, float ry,
+                                                      float ifx, float ify, const float4& cur, float4& last,
+                                                      float4* cand) {
+  int best_n = -1;
+  float best_c = kCostInf;
+  if (r < 4) {
+    for (int k = 0; k < 7; ++k) {
+      const int nx_ = x + c_near[r][k][0], ny_ = y + c_near[r][k][1];
+      if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
+      const float c = J.cost[ny_ * J.w + nx_];
+      if (c < best_c) {
+        best_c = c;
+        best_n = ny_ * J.w + nx_;
+      }
+    }
+  } else {
+    const int d = r - 4;
+    const int sx = d == 2 ? -1 : (d == 3 ? 1 : 0);
+    const int sy = d == 0 ? -1 : (d == 1 ? 1 : 0);
+    for (int k = 0; k < 11; ++k) {
+      const int off = 3 + 2 * k;
+      const int nx_ = x + sx * off, ny_ = y + sy * off;
+      if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
+      const float c = J.cost[ny_ * J.w + nx_];
+      if (c < best_c) {
+        best_c = c;
+        best_n = ny_ * J.w + nx_;
+      }
+    }
+  }
+  if (best_n < 0 || best_c >= kCostInf) return false;
+  const float4 hn = J.hyp[best_n];
+  const int nxp = best_n % J.w, nyp = best_n / J.w;
+  float rho;
+  plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
+  if (!(rho > 0.f)) return false;
+  if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) return false;
+  if (J.prune && hn.y == last.y && hn.z == last.z && hn.w == last.w && rho == last.x) return false;
+  last = make_float4(rho, hn.y, hn.z, hn.w);
+  *cand = last;
+  return true;
+}
+
+// Refinement candidate k (0-4) around the current plane `cur`: a random
+// plane (k = 0), the inverse depth perturbed (k = 1), the normal perturbed
+// (k = 2), both (k = 3) -- ranges shrinking by half per iteration (`scale`)
+// -- and the current depth on a fronto-parallel plane (k = 4, the reference's
+// model; false when the plane already is one).
+__device__ __forceinline__ bool refinement_candidate(const Job& J, Rng& g, int k, const float4& cur, float rx,
+                                                     float ry, float scale, float span, float4* cand) {
+  float rho = cur.x, nx = cur.y, ny = cur.z, nz = cur.w;
+  if (k == 0) {
+    rho = J.rho_min + span * g.uniform();
+    random_normal(g, rx, ry, &nx, &ny, &nz);
+  } else if (k == 4) {
+    if (nx == 0.f && ny == 0.f) return false;
+    nx = 0.f;
+    ny = 0.f;
+    nz = -1.f;
+  } else {
+    if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
+    if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
+  }
+  *cand = make_float4(rho, nx, ny, nz);
+  return true;
+}
+
+// The evaluation counters of a warp into the job's counter (one atomic per
+// warp and counter).
+__device__ __forceinline__ void add_counts(const Job& J, unsigned int mask, const int* counts, int n) {
+  for (int i = 0; i < n; ++i) {
+    const unsigned int v = __reduce_add_sync(mask, (unsigned int)counts[i]);
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1) && v) atomicAdd(J.eval_counter + i, (unsigned long long)v);
+  }
+}
+
 // One red-black half-sweep of one pixel: propagation from the best-cost
 // neighbour of each of the 8 adaptive regions, then 5 refinement hypotheses.
 template <int H, int kMode, class RefT>
@@ -450,93 +550,32 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
   int counts[2] = {0, 0};  // hypotheses, source windows sampled
 
   float4 last = make_float4(-1.f, 0.f, 0.f, 0.f);  // the last candidate evaluated
-  // --- propagation: best-cost neighbour of each region ---
   for (int r = 0; r < 8; ++r) {
-    int best_n = -1;
-    float best_c = kCostInf;
-    if (r < 4) {
-      for (int k = 0; k < 7; ++k) {
-        const int nx_ = x + c_near[r][k][0], ny_ = y + c_near[r][k][1];
-        if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
-        const float c = J.cost[ny_ * J.w + nx_];
-        if (c < best_c) {
-          best_c = c;
-          best_n = ny_ * J.w + nx_;
-        }
-      }
-    } else {
-      const int d = r - 4;
-      const int sx = d == 2 ? -1 : (d == 3 ? 1 : 0);
-      const int sy = d == 0 ? -1 : (d == 1 ? 1 : 0);
-      for (int k = 0; k < 11; ++k) {
-        const int off = 3 + 2 * k;
-        const int nx_ = x + sx * off, ny_ = y + sy * off;
-        if (nx_ < 0 || ny_ < 0 || nx_ >= J.w || ny_ >= J.h) continue;
-        const float c = J.cost[ny_ * J.w + nx_];
-        if (c < best_c) {
-          best_c = c;
-          best_n = ny_ * J.w + nx_;
-        }
-      }
-    }
-    if (best_n < 0 || best_c >= kCostInf) continue;
-    const float4 hn = J.hyp[best_n];
-    const int nxp = best_n % J.w, nyp = best_n / J.w;
-    float rho;
-    plane_candidate_transfer(hn, ((float)nxp + 0.5f - J.rcx) * ifx, ((float)nyp + 0.5f - J.rcy) * ify, rx, ry, &rho);
-    if (!(rho > 0.f)) continue;
-    // the current plane again (same normal, inverse depth within rounding of
-    // the transfer): nothing to learn -- in a converged region most regions
-    // propose exactly this
-    if (hn.y == cur.y && hn.z == cur.z && hn.w == cur.w && fabsf(rho - cur.x) <= kSamePlaneRel * cur.x) continue;
-    // the previous region's candidate again (the same plane reached through
-    // another neighbour): it was rejected, and its cost has not changed
-    if (J.prune && hn.y == last.y && hn.z == last.z && hn.w == last.w && rho == last.x) continue;
-    last = make_float4(rho, hn.y, hn.z, hn.w);
-    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, hn.y, hn.z, hn.w, rw, ref, nullptr, counts,
-                                               J.prune ? cur_cost : kCostInf);
+    float4 cand;
+    if (!propagation_candidate(J, x, y, r, rx, ry, ifx, ify, cur, last, &cand)) continue;
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, cand.x, cand.y, cand.z, cand.w, rw, ref, nullptr,
+                                               counts, J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
-      cur = make_float4(rho, hn.y, hn.z, hn.w);
+      cur = cand;
       cur_sup = c.support;
     }
   }
-
-  // --- refinement: random and perturbed hypotheses, shrinking with iterations ---
   Rng g = pixel_rng(J, idx, iter, 2 + color);
   const float scale = exp2f(-(float)iter);  // 1, 1/2, 1/4, ...
   const float span = J.rho_max - J.rho_min;
   for (int k = 0; k < 5; ++k) {
-    float rho = cur.x, nx = cur.y, ny = cur.z, nz = cur.w;
-    if (k == 0) {
-      rho = J.rho_min + span * g.uniform();
-      random_normal(g, rx, ry, &nx, &ny, &nz);
-    } else if (k == 4) {
-      // the current depth on a fronto-parallel plane (the reference's model)
-      if (nx == 0.f && ny == 0.f) continue;
-      nx = 0.f;
-      ny = 0.f;
-      nz = -1.f;
-    } else {
-      if (k & 1) rho = cur.x + 0.25f * span * scale * g.sym();
-      if (k & 2) perturb_normal(g, rx, ry, 0.5f * scale, &nx, &ny, &nz);
-    }
-    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, rho, nx, ny, nz, rw, ref, nullptr, counts, J.prune ? cur_cost : kCostInf);
+    float4 cand;
+    if (!refinement_candidate(J, g, k, cur, rx, ry, scale, span, &cand)) continue;
+    const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, cand.x, cand.y, cand.z, cand.w, rw, ref, nullptr,
+                                               counts, J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
       cur_cost = c.cost;
-      cur = make_float4(rho, nx, ny, nz);
+      cur = cand;
       cur_sup = c.support;
     }
   }
-  if (J.eval_counter) {
-    const unsigned int m = __activemask();
-    const unsigned int hyps = __reduce_add_sync(m, (unsigned int)counts[0]);
-    const unsigned int wins = __reduce_add_sync(m, (unsigned int)counts[1]);
-    if ((threadIdx.x & 31) == (__ffs(m) - 1)) {
-      atomicAdd(J.eval_counter, (unsigned long long)hyps);
-      atomicAdd(J.eval_counter + 1, (unsigned long long)wins);
-    }
-  }
+  if (J.eval_counter) add_counts(J, __activemask(), counts, 2);
   J.hyp[idx] = cur;
   J.cost[idx] = cur_cost;
   J.support[idx] = (uint8_t)min(cur_sup, 255);
@@ -581,6 +620,158 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
 
 constexpr int kTmaWaitPolls = 1 << 22;
 
+// ---- the staged-window schedule ----
+// The 2-D box {x, y} of `map` (a tensor map in global memory) into shared
+// memory, completion signalled on `bar`.  x is even (8-byte elements:
+// 16-byte aligned rows); x or y may be negative or past the end (zeros).
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int x, int y, uint64_t* bar,
+                                            uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// One warp's source box and its copy state (the same in every lane).
+struct WarpBox {
+  float2* box;     // kStageH rows x kStageW texel pairs, 128-byte aligned
+  uint64_t* bar;   // the box's mbarrier (arrival count 1)
+  uint32_t phase;  // parity of the next copy's completion
+  int polls;       // wait limit
+  int* err;        // set when a wait runs out
+  bool dead;       // a wait ran out: no further copies into this box in this launch
+};
+
+// One source view of one candidate for the whole warp (every lane calls it;
+// `act`: this lane's hypothesis is live for the view).  The lanes whose
+// windows lie fully inside the source (the fast path) pool the texels they
+// read -- the corners' footprints with a margin of one texel for rounding --
+// into one box; when it fits kStageW x kStageH, lane 0 copies it from the
+// view's pair image by TMA and every lane waits (bounded) for it, then those
+// windows are read from shared memory.  Other windows, and full ones whose
+// box does not fit, read the texture.  Either way a window's NCC is the same
+// bit for bit.
+template <int H, class Ref>
+__device__ __forceinline__ ViewResult eval_view_staged(const Job& J, const SrcView& S, int x, int y, const ff P[3],
+                                                       const PlaneHyp& hp, bool act, const RefWindow& rw,
+                                                       const Ref& ref, WarpBox& wb, int* counts) {
+  WindowPlace g;
+  const bool geo = act && place_window<H>(J, S, P, hp, rw, &g);
+  int x0 = 0x7fffffff, x1 = (int)0x80000000, y0 = 0x7fffffff, y1 = (int)0x80000000;
+  if (geo && g.full) {
+    // footprints of index coordinates in [min, max]: texels floor(min) - 1 ..
+    // floor(max) + 1 (an exact tie reads one texel lower), plus the margin
+    x0 = g.iu + (int)floorf(g.umin) - 2;
+    x1 = g.iu + (int)floorf(g.umax) + 2;
+    y0 = g.iv + (int)floorf(g.vmin) - 2;
+    y1 = g.iv + (int)floorf(g.vmax) + 2;
+  }
+  x0 = __reduce_min_sync(0xffffffffu, x0);
+  x1 = __reduce_max_sync(0xffffffffu, x1);
+  y0 = __reduce_min_sync(0xffffffffu, y0);
+  y1 = __reduce_max_sync(0xffffffffu, y1);
+  const int ax = x0 & ~1;  // an even first pair: 16-byte TMA rows
+  // pair element e of a box row holds texels ax + e and ax + e + 1, so the
+  // texels ax .. x1 need x1 - ax <= kStageW; rows y0 .. y1 need kStageH
+  bool staged = S.pair_map != nullptr && !wb.dead && x0 <= x1 && x1 - ax <= kStageW && y1 - y0 < kStageH;
+  if (staged) {
+    if ((threadIdx.x & 31) == 0) tma_load_2d(wb.box, S.pair_map, ax, y0, wb.bar, (uint32_t)kStageBytes);
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(wb.bar, wb.phase, wb.polls));
+    wb.phase ^= 1u;
+    if (!ok) {
+      // the copy may still land: the box is not used again in this launch
+      wb.dead = true;
+      staged = false;
+      if ((threadIdx.x & 31) == 0) atomicExch(wb.err, 1);
+    }
+  }
+  ViewResult v{0.0f, -1};
+  if (geo) {
+    if (staged && g.full) {
+      v = eval_view_box<H>(J, g, rw, ref, wb.box, ax, y0);
+      ++counts[2];
+    } else {
+      v = eval_view_placed<H, kSrcExact>(J, S, x, y, g, hp, rw, ref);
+    }
+  }
+  __syncwarp();  // every lane is done with the box before the next copy into it
+  return v;
+}
+
+// eval_plane_hyp for the staged schedule: the view loop runs in step across
+// the warp (J is the same for the whole block); `have` = this lane has a
+// candidate in this slot.
+template <int H, class Ref>
+__device__ __forceinline__ HypCost eval_plane_hyp_staged(const Job& J, const PCache& pc, int x, int y, float rx,
+                                                         float ry, const float4& cand, bool have, const RefWindow& rw,
+                                                         const Ref& ref, int* counts, float beat, WarpBox& wb) {
+  PlaneHyp hp;
+  const float rho = cand.x;
+  const bool live = have && rho > 0.0f && !(rho < J.rho_min) && !(rho > J.rho_max) &&
+                    make_plane_hyp(J, rx, ry, rho, cand.y, cand.z, cand.w, &hp);
+  if (live) ++counts[0];
+  return plane_hyp_cost<true>(
+      J, live,
+      [&](int s, bool act) {
+        ff P[3] = {};
+        if (act) pc.get(s, P);
+        return eval_view_staged<H>(J, J.src[s], x, y, P, hp, act, rw, ref, wb, counts);
+      },
+      nullptr, counts, beat);
+}
+
+// sweep_pixel for the staged schedule: every lane of the warp runs every
+// candidate slot and view in step; a lane outside the image, or without a
+// candidate in a slot, only takes part in the warp's collective steps.
+template <int H, class RefT>
+__device__ __forceinline__ void sweep_pixel_staged(const Job& J, const PCache& pc, const RefT& ref, bool inside,
+                                                   int x, int y, int color, int iter, WarpBox& wb) {
+  const int idx = inside ? y * J.w + x : 0;
+  RefWindow rw{0.0f, 0.0f, false};
+  float rx = 0.f, ry = 0.f;
+  float4 cur = make_float4(0.f, 0.f, 0.f, 0.f);
+  float cur_cost = kCostInf;
+  int cur_sup = 0;
+  if (inside) {
+    rw = tile_window<H>(J, ref, x, y);
+    fill_pcache(J, pc, x, y, &rx, &ry);
+    cur = J.hyp[idx];
+    cur_cost = J.cost[idx];
+    cur_sup = J.support[idx];
+  }
+  const float ifx = 1.0f / J.rfx, ify = 1.0f / J.rfy;
+  int counts[3] = {0, 0, 0};  // hypotheses, source windows sampled, of them read from a staged box
+  float4 last = make_float4(-1.f, 0.f, 0.f, 0.f);
+  Rng g{0};
+  const float scale = exp2f(-(float)iter);
+  const float span = J.rho_max - J.rho_min;
+  // slots 0-7: propagation regions; 8-12: refinement candidates (one loop,
+  // so that the hypothesis evaluation is instantiated once)
+  for (int slot = 0; slot < 13; ++slot) {
+    if (slot == 8) g = pixel_rng(J, idx, iter, 2 + color);
+    float4 cand = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool have = inside && (slot < 8 ? propagation_candidate(J, x, y, slot, rx, ry, ifx, ify, cur, last, &cand)
+                                          : refinement_candidate(J, g, slot - 8, cur, rx, ry, scale, span, &cand));
+    const HypCost c = eval_plane_hyp_staged<H>(J, pc, x, y, rx, ry, cand, have, rw, ref, counts,
+                                               J.prune ? cur_cost : kCostInf, wb);
+    if (have && c.cost < cur_cost) {
+      cur_cost = c.cost;
+      cur = cand;
+      cur_sup = c.support;
+    }
+  }
+  if (J.eval_counter) add_counts(J, 0xffffffffu, counts, 3);
+  if (inside) {
+    J.hyp[idx] = cur;
+    J.cost[idx] = cur_cost;
+    J.support[idx] = (uint8_t)min(cur_sup, 255);
+  }
+}
+
 // One red-black half-sweep over a whole batch: a persistent kernel (grid =
 // resident blocks) whose blocks pull work items -- 64-column x R-row tiles,
 // R = blockDim.y -- from an atomic counter until the batch is exhausted.  A
@@ -593,22 +784,41 @@ constexpr int kTmaWaitPolls = 1 << 22;
 // same-colour pixels (16 x 4 pixels for R >= 4).  Each window sample of a
 // warp is one texture instruction over its 32 pixels, and their source
 // footprints then cluster in a 2-D patch of the source instead of spreading
-// along a 64-pixel row: fewer texture-cache lines per instruction.  `queue` is this launch's work counter
-// (zeroed by the init kernel); `total` its item count -- jobs with fewer
-// iterations than `iter + 1` sit at the end of the job order and fall
-// outside it.
-template <int H, int kMode>
-__global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch B, int total, int* queue, int color,
+// along a 64-pixel row: fewer texture-cache lines per instruction.  `queue`
+// is this launch's work counter (zeroed by the init kernel); `total` its item
+// count -- jobs with fewer iterations than `iter + 1` sit at the end of the
+// job order and fall outside it.
+//
+// kStaged (exact interpolation, H > 0): the staged-window schedule -- each
+// warp owns a kStageW x kStageH box of texel pairs at the start of the
+// dynamic shared memory (the source-ray cache follows it) and reads the
+// windows its pixels share from there (eval_view_staged).
+template <int H, int kMode, bool kStaged>
+__global__ void __maxnreg__(kStaged ? 128 : 96) k_plane_sweep(const __grid_constant__ PlaneBatch B, int total, int* queue, int color,
                                               int iter) {
+  static_assert(!kStaged || (H > 0 && kMode == kSrcExact), "the staged schedule reads exact 2x2 footprints");
   extern __shared__ float2 smem[];
   constexpr int kHalo = H > 0 ? H : 1;
   __shared__ __align__(128) float tile[2 * (kMaxTileRows + 2 * kHalo) * kTileCols];
   __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t box_bar[kStaged ? kMaxTileRows : 1];
   __shared__ int s_item;
   const int R = (int)blockDim.y;
   const int nthreads = 32 * R;
   const int tid = threadIdx.y * 32 + threadIdx.x;
-  const PCache pc{smem, nthreads, tid};
+  float2* pc_base = smem;
+  WarpBox wb{nullptr, nullptr, 0u, 0, B.err, false};
+  if constexpr (kStaged) {
+    // the boxes first, from the first 128-byte boundary (TMA destinations)
+    const uint32_t a = smem_addr(smem);
+    char* boxes = reinterpret_cast<char*>(smem) + (((a + 127u) & ~127u) - a);
+    wb.box = reinterpret_cast<float2*>(boxes + (size_t)threadIdx.y * kStageBytes);
+    wb.bar = &box_bar[threadIdx.y];
+    wb.polls = B.tma_poll_limit > 0 ? B.tma_poll_limit : kTmaWaitPolls;
+    pc_base = reinterpret_cast<float2*>(boxes + (size_t)R * kStageBytes);
+    if (threadIdx.x == 0) mbar_init(wb.bar, 1);
+  }
+  const PCache pc{pc_base, nthreads, tid};
   const int box_rows = R + 2 * H;
   // this thread's pixel in the tile: row ty, same-colour column pair `pair`.
   // A warp covers RW rows x PW pairs; within it each quad of lanes (the
@@ -667,7 +877,13 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
         break;
       }
     }
-    if (x < J.w && y < J.h) {
+    const bool inside = x < J.w && y < J.h;
+    if constexpr (kStaged) {
+      const float* plane0 = tile;
+      const float* plane1 = tile + box_rows * kTileCols;
+      const TileRef ref{parity ? plane1 : plane0, parity ? plane0 : plane1, pair, parity, ty};
+      sweep_pixel_staged<H>(J, pc, ref, inside, x, y, color, iter + J.iter_offset, wb);
+    } else if (inside) {
       if constexpr (H > 0) {
         const float* plane0 = tile;
         const float* plane1 = tile + box_rows * kTileCols;
@@ -681,6 +897,11 @@ __global__ void __maxnreg__(96) k_plane_sweep(const __grid_constant__ PlaneBatch
       }
     }
     __syncthreads();
+  }
+  if constexpr (kStaged) {
+    // a box copy whose wait ran out gets one more bounded chance to land
+    // before the block's shared memory is released
+    if (wb.dead && threadIdx.x == 0) mbar_wait(wb.bar, wb.phase ^ 1u, wb.polls);
   }
 }
 
@@ -1367,10 +1588,29 @@ cudaError_t launch_plane_init(const PlaneBatch& B, int patch_half, int mode, int
   });
 }
 
-cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int* blocks_per_sm) {
-  const size_t sm = pcache_bytes(max_src, 32 * rows);
+// The staged schedule's dynamic shared memory: the warps' boxes (after up to
+// 128 bytes of alignment) and then the source-ray cache.
+static size_t sweep_smem_bytes(int max_src, int rows, bool staged) {
+  return pcache_bytes(max_src, 32 * rows) + (staged ? 128 + (size_t)rows * kStageBytes : 0);
+}
+
+// Calls f(kernel) for the sweep instance of (window, mode, schedule).
+template <class F>
+static cudaError_t dispatch_sweep(int patch_half, int mode, int staged, F&& f) {
+  if (staged) {
+    if (mode != kSrcExact) return cudaErrorInvalidValue;
+    if (patch_half == 5) return f(k_plane_sweep<5, kSrcExact, true>);
+    if (patch_half == 3) return f(k_plane_sweep<3, kSrcExact, true>);
+    return cudaErrorInvalidValue;
+  }
   return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
-    auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
+    return f(k_plane_sweep<decltype(h)::value, decltype(k)::value, false>);
+  });
+}
+
+cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int rows, int staged, int* blocks_per_sm) {
+  const size_t sm = sweep_smem_bytes(max_src, rows, staged != 0);
+  return dispatch_sweep(patch_half, mode, staged, [&](auto* fn) {
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 32 * rows, sm);
@@ -1378,17 +1618,31 @@ cudaError_t plane_sweep_occupancy(int patch_half, int mode, int max_src, int row
 }
 
 cudaError_t launch_plane_sweep(const PlaneBatch& B, int total, int* queue, int patch_half, int mode, int max_src,
-                               int rows, int grid, int color, int iter, cudaStream_t st) {
+                               int rows, int staged, int grid, int color, int iter, cudaStream_t st) {
   if (total <= 0) return cudaSuccess;
   if (rows < 1 || rows > kMaxTileRows || grid < 1 || total > B.start[B.njobs]) return cudaErrorInvalidValue;
-  const size_t sm = pcache_bytes(max_src, 32 * rows);
-  return dispatch_plane(patch_half, mode, [&](auto h, auto k) {
-    auto* fn = k_plane_sweep<decltype(h)::value, decltype(k)::value>;
+  const size_t sm = sweep_smem_bytes(max_src, rows, staged != 0);
+  return dispatch_sweep(patch_half, mode, staged, [&](auto* fn) {
     cudaError_t e = allow_smem(fn, sm);
     if (e != cudaSuccess) return e;
     fn<<<grid, dim3(32, rows), sm, st>>>(B, total, queue, color, iter);
     return cudaGetLastError();
   });
+}
+
+__global__ void k_pair_image(cudaTextureObject_t tex, int w, int h, float2* out, int pitch) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const float a = tex2D<float>(tex, (float)x + 0.5f, (float)y + 0.5f);
+  const float b = x + 1 < w ? tex2D<float>(tex, (float)x + 1.5f, (float)y + 0.5f) : 0.0f;
+  out[(size_t)y * pitch + x] = make_float2(a, b);
+}
+
+cudaError_t launch_pair_image(cudaTextureObject_t tex, int w, int h, float2* out, int pitch, cudaStream_t st) {
+  if (w < 1 || h < 1 || pitch < w) return cudaErrorInvalidValue;
+  const dim3 b(32, 8);
+  k_pair_image<<<grid2d(w, h, b), b, 0, st>>>(tex, w, h, out, pitch);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_plane_refine(const PlaneBatch& B, int patch_half, int mode, int max_src, cudaStream_t st) {

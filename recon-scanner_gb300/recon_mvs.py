@@ -83,7 +83,7 @@ class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("storage", C.c_int32), ("best_k", C.c_int32), ("refine", C.c_int32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("sampling", C.c_int32), ("prefilter", C.c_int32),
                 ("interp", C.c_int32), ("tile_rows", C.c_int32), ("per_view", C.c_int32),
-                ("exhaustive", C.c_int32), ("coarse_iterations", C.c_int32)]
+                ("exhaustive", C.c_int32), ("coarse_iterations", C.c_int32), ("window_staging", C.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -145,8 +145,8 @@ class TsdfConfig(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("hypotheses_evaluated", C.c_uint64), ("last_run_ms", C.c_double), ("last_sweep_ms", C.c_double),
                 ("last_sweep_launches", C.c_int32), ("tile_rows", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("reserved", C.c_int32 * 1),
-                ("windows_evaluated", C.c_uint64)]
+                ("graph_launches", C.c_int32), ("tune_trials", C.c_int32), ("window_staging", C.c_int32),
+                ("windows_evaluated", C.c_uint64), ("windows_staged", C.c_uint64)]
 
 
 CANCEL_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p)
