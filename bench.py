@@ -728,14 +728,17 @@ KERNEL_SOURCES = ["pm.cu", "cost.cuh", "common.cuh", "adjoint.cuh", "kernels.h"]
 
 
 def kernel_sources_digest():
-    """Digest of the sweep's kernel sources: a profile taken on other
-    sources does not describe the kernel this run times."""
+    """Digest of the sweep's kernel sources and of the build recipe (its
+    compiler flags): a profile taken on other sources or flags does not
+    describe the kernel this run times."""
     import hashlib
 
     h = hashlib.sha256()
     for name in KERNEL_SOURCES:
         with open(os.path.join(ROOT, "recon-scanner_gb300", "csrc", name), "rb") as f:
             h.update(f.read())
+    with open(os.path.join(ROOT, "recon-scanner_gb300", "build.py"), "rb") as f:
+        h.update(f.read())
     return h.hexdigest()[:16]
 
 
