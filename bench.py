@@ -399,8 +399,8 @@ def run_reference_arm(args):
                              "sample": smp.describe(len(runs), measured)},
             "e2e": {"value": value, "unit": "depth maps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if WORKLOAD == "c2":
-        # one whole map 0 timed once against the tile estimate of the same
-        # host (profiles/reference_cpu_tabletop1920.md)
+        # one whole map 0 of the reference's own code (its release build, 8
+        # x86 threads), timed once against the tile estimate of the same host
         line["extrapolation_check"] = {
             "full_map_s": 3216.1, "tile_estimate_s_48_tiles": 2739.4, "rel_err_48_tiles": -0.148,
             "rel_err_4_10_20_tiles": [-0.306, -0.221, -0.240],
