@@ -16,7 +16,10 @@ staged; the capture's consistency + fusion stage is reported beside it.
             the adjoint, coarse-to-fine initialisation (iterations 1-2 of the
             8 on the half-resolution pyramid level, as the reference design
             lays out its search: level 1 for the coarse rounds, level 0 for
-            the fine ones); the plain path (FP32 textures, exact FP32
+            the fine ones), and an exploration schedule (the random and
+            fronto-parallel candidates in iterations 1-3 only, the search's
+            propagation and local perturbations in all 8); the plain path
+            (FP32 textures, exact FP32
             interpolation, one launch per view, the reference's
             golden-section refinement, all 8 iterations at full resolution)
             is timed in the same run and reported under "plain" with its
@@ -589,11 +592,12 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
              ("batched_fp16_exact_gauss_newton", True, 0, 2, 0, 1),
              ("batched_fp16_exact_gauss_newton_staged_windows", True, 0, 2, 0, 2),
              ("batched_fp16_exact_gauss_newton_staged_windows_coarse_to_fine", True, 0, 2, args.coarse, 2),
-             ("batched_fp16_texture_gauss_newton_full_resolution", True, 1, 2, 0, 1)]
+             ("batched_fp16_texture_gauss_newton_full_resolution", True, 1, 2, 0, 1),
+             ("batched_fp16_texture_gauss_newton_coarse_to_fine", True, 1, 2, args.coarse, 1)]
     out = {"steps": args.attr_steps, "forms": {}}
     exact_maps = None
     for name, fp16, interp, refine, coarse, staging in forms:
-        ms, _, _, _, fmaps, fst = time_form(M, views, cfgs, mk(fp16, interp, False, refine, coarse, staging),
+        ms, _, _, _, fmaps, fst = time_form(M, views, cfgs, mk(fp16, interp, False, refine, coarse, staging, 0),
                                             args.attr_steps, 1, flush, world, undistort, scenes=scenes)
         tot = barrier_max(world, float(sum(ms)))
         med, p95 = agreement(fmaps, chosen_maps)
@@ -643,8 +647,9 @@ def attribution(M, views, cfgs, mk, args, flush, world, undistort, scenes, truth
     out["cost_vs_fp64_oracle"] = cost
     out["note"] = ("plain = FP32 storage, exact interpolation, one launch per view, golden section, every iteration "
                    "at full resolution; each form adds one change: batched, FP16 storage, Gauss-Newton, texture-unit "
-                   "interpolation (8-bit weights); chosen adds coarse-to-fine (the first iterations on the "
-                   "half-resolution level, the same total).  Beside the chain: the exact Gauss-Newton form with "
+                   "interpolation (8-bit weights), coarse-to-fine (the first iterations on the half-resolution "
+                   "level, the same total); chosen adds the exploration schedule (the random and fronto-parallel "
+                   "candidates only in the first iterations).  Beside the chain: the exact Gauss-Newton form with "
                    "its source windows staged in shared memory by TMA (window_staging = 2; the same maps as its "
                    "texture reads, bit for bit), alone and with coarse-to-fine")
     return out
@@ -789,10 +794,12 @@ def run_gpu(args):
     s_eff = float(np.dot(pixels, n_src) / np.sum(pixels))
     # FLOP model: per source window sampled K*K*26 + 30, per hypothesis 40
     flop_per_window, flop_per_hyp_setup = K * K * 26 + 30, 40
-    mk = lambda fp16, interp, per_view, refine, coarse=args.coarse, staging=args.window_staging: M.Options(
-        mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
-        refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp, per_view=int(per_view),
-        tile_rows=args.tile_rows, coarse_iterations=coarse, window_staging=staging if interp == 0 else 0)
+    mk = lambda fp16, interp, per_view, refine, coarse=args.coarse, staging=args.window_staging, \
+        explore=args.exploration: M.Options(
+            mode=M.MODE_PLANE, best_k=args.best_k, storage=M.STORAGE_FP16 if fp16 else M.STORAGE_FP32, device=local,
+            refine=refine, prefilter=int(args.prefilter), sampling=args.sampling, interp=interp,
+            per_view=int(per_view), tile_rows=args.tile_rows, coarse_iterations=coarse,
+            window_staging=staging if interp == 0 else 0, exploration_iterations=explore)
     opts = mk(args.fp16, args.interp, args.per_view, args.refine)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -809,7 +816,7 @@ def run_gpu(args):
     if not args.plain and not args.chosen_only:
         p_fp16 = False if WORKLOAD != "c3" else args.fp16
         p_interp = 0 if WORKLOAD != "c3" else args.interp
-        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True, 1, 0), args.steps,
+        p_ms, _, _, p_launches, p_maps, _ = time_form(M, views, cfgs, mk(p_fp16, p_interp, True, 1, 0, explore=0), args.steps,
                                                       args.warmup, flush, world, undistort, scenes=scenes)
         p_total = barrier_max(world, float(sum(p_ms)))
         med, p95 = agreement(maps, p_maps)
@@ -884,7 +891,9 @@ def run_gpu(args):
             f"interpolation, {'one launch per view' if args.per_view else 'batched persistent launch, CUDA graph'}, "
             f"{'Gauss-Newton (adjoint) refinement' if args.refine == 2 else 'golden-section refinement'}"
             + (f", coarse-to-fine: iterations 1-{args.coarse} of {ITERS} on the half-resolution level (2x2 means)"
-               if args.coarse else ", every iteration at full resolution"))
+               if args.coarse else ", every iteration at full resolution")
+            + (f", exploration candidates (random, fronto-parallel) in iterations 1-{args.exploration} only"
+               if args.exploration else ""))
     wl = describe_workload(scenes)
     line = {"metric": METRIC, "value": value, "unit": "depth maps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -892,7 +901,8 @@ def run_gpu(args):
             "data": "synthetic (seeded scenes, analytic truth)",
             "config": {"workload": f"{wl}; {K}x{K}, {ITERS} iterations, plane mode, best_k={args.best_k}",
                        "maps_per_step": n_maps, "megapixels_per_step": sum(pixels) / 1e6,
-                       "form": form, "coarse_iterations": args.coarse, "tile_rows": st.tile_rows,
+                       "form": form, "coarse_iterations": args.coarse,
+                       "exploration_iterations": args.exploration, "tile_rows": st.tile_rows,
                        "ctas_per_sm": st.ctas_per_sm,
                        "prefilter": bool(args.prefilter), "sampling": args.sampling,
                        "l2": "flushed between steps (512 MiB write, outside the timed events)",
@@ -1324,6 +1334,9 @@ def main():
     ap.add_argument("--coarse", type=int, default=None,
                     help="coarse-to-fine: the first N of the iterations on the half-resolution level (chosen form "
                          "default 2, the reference design's rounds 1-2 on pyramid level 1; 0 = off)")
+    ap.add_argument("--exploration", type=int, default=None,
+                    help="exploration schedule: the random and fronto-parallel candidates in the first N iterations "
+                         "only (chosen form default: the coarse iterations + 1; 0 = every iteration)")
     args = ap.parse_args()
     set_workload(args.workload)
     if args.depth_range:
@@ -1335,6 +1348,8 @@ def main():
         args.refine = 1 if (args.plain or args.workload == "c3") else 2
     if args.coarse is None:
         args.coarse = 0 if (args.plain or args.workload == "c3") else 2
+    if args.exploration is None:
+        args.exploration = 0 if (args.plain or args.workload == "c3" or not args.coarse) else args.coarse + 1
     if args.plain:
         args.fp16, args.interp, args.per_view = False, 0, True
     elif args.workload == "c3":

@@ -171,6 +171,12 @@ typedef struct recon_mvs_options {
                                 cover (up to 40 x 24 texel pairs) into shared memory by TMA and
                                 samples it there, windows whose box does not fit read the texture.  The
                                 maps are the same bit for bit in every schedule */
+  int32_t exploration_iterations; /* plane mode exploration schedule: 0 = every sweep evaluates the two
+                                exploration candidates (a uniformly random plane; the current depth on a
+                                fronto-parallel plane); n > 0 = only iterations 0 .. n-1 (counted over the
+                                whole schedule, coarse-to-fine levels included) do, later sweeps keep
+                                propagation and the local perturbations.  The random draws are made
+                                either way, so iterations before n are unchanged */
 } recon_mvs_options;
 
 /* Inputs of one reference view: the PatchMatchStereo argument list

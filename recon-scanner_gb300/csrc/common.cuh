@@ -239,6 +239,11 @@ struct Job {
   int coarse_w, coarse_h;
   float crfx, crfy, crcx, crcy;  // the half-resolution reference intrinsics
   int iter_offset;               // iterations run at the coarse level: the schedule continues from there
+  // exploration schedule: sweeps of iteration >= explore_iters (counted over
+  // the whole schedule) evaluate no exploration candidate (the uniformly
+  // random plane, the current depth on a fronto-parallel plane); 0 = every
+  // iteration does
+  int explore_iters;
 };
 
 // Per-pixel ray of the reference camera, FP64: pinhole fast path, or the

@@ -326,6 +326,7 @@ struct Context {
       fail(RECON_ERR_INVALID_ARGUMENT, "U8 storage needs plane mode");
     if (o.storage == RECON_MVS_STORAGE_BF16 && (o.mode != RECON_MVS_MODE_PLANE || o.interp != 0))
       fail(RECON_ERR_INVALID_ARGUMENT, "BF16 storage needs plane mode with exact interpolation (interp = 0)");
+    if (o.exploration_iterations < 0) fail(RECON_ERR_INVALID_ARGUMENT, "exploration_iterations < 0");
     if (o.window_staging < 0 || o.window_staging > 2)
       fail(RECON_ERR_INVALID_ARGUMENT, "window_staging must be 0 (autotuned), 1 (off) or 2 (on)");
     if (o.window_staging == 2 &&
@@ -817,6 +818,7 @@ static std::unique_ptr<JobData> build_job_data(Context& C, const std::shared_ptr
   J.photo_threshold = (float)cfg->photo_threshold;
   J.best_k = C.opts.best_k;
   J.prune = C.opts.exhaustive ? 0 : 1;
+  J.explore_iters = C.opts.exploration_iterations;
   J.seed = C.opts.seed;
   // the counters measure the full-resolution sweeps (the roofline's launches);
   // a coarse level's sweeps are not counted

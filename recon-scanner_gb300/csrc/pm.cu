@@ -506,7 +506,9 @@ __device__ __forceinline__ bool propagation_candidate(const Job& J, int x, int y
 // plane (k = 0), the inverse depth perturbed (k = 1), the normal perturbed
 // (k = 2), both (k = 3) -- ranges shrinking by half per iteration (`scale`)
 // -- and the current depth on a fronto-parallel plane (k = 4, the reference's
-// model; false when the plane already is one).
+// model; false when the plane already is one).  The draws are made whether
+// or not the candidate is then evaluated (exploring()), so the random stream
+// of every pixel is the same under any exploration schedule.
 __device__ __forceinline__ bool refinement_candidate(const Job& J, Rng& g, int k, const float4& cur, float rx,
                                                      float ry, float scale, float span, float4* cand) {
   float rho = cur.x, nx = cur.y, ny = cur.z, nz = cur.w;
@@ -524,6 +526,16 @@ __device__ __forceinline__ bool refinement_candidate(const Job& J, Rng& g, int k
   }
   *cand = make_float4(rho, nx, ny, nz);
   return true;
+}
+
+// Whether iteration `iter` evaluates refinement candidate k: the exploration
+// candidates (k = 0, the random plane; k = 4, the fronto-parallel plane) stop
+// at the job's explore_iters -- by then the search has converged and they
+// almost never win (at 1920x1440 after coarse-to-fine initialisation: the
+// random plane 0.04-0.4 % of its evaluations, the fronto-parallel plane
+// 0.2-2.4 %) -- while propagation and the local perturbations go on.
+__device__ __forceinline__ bool exploring(const Job& J, int k, int iter) {
+  return (k != 0 && k != 4) || J.explore_iters <= 0 || iter < J.explore_iters;
 }
 
 // The evaluation counters of a warp into the job's counter (one atomic per
@@ -566,7 +578,7 @@ __device__ __forceinline__ void sweep_pixel(const Job& J, const PCache& pc, cons
   const float span = J.rho_max - J.rho_min;
   for (int k = 0; k < 5; ++k) {
     float4 cand;
-    if (!refinement_candidate(J, g, k, cur, rx, ry, scale, span, &cand)) continue;
+    if (!refinement_candidate(J, g, k, cur, rx, ry, scale, span, &cand) || !exploring(J, k, iter)) continue;
     const HypCost c = eval_plane_hyp<H, kMode>(J, pc, x, y, rx, ry, cand.x, cand.y, cand.z, cand.w, rw, ref, nullptr,
                                                counts, J.prune ? cur_cost : kCostInf);
     if (c.cost < cur_cost) {
@@ -754,8 +766,10 @@ __device__ __forceinline__ void sweep_pixel_staged(const Job& J, const PCache& p
   for (int slot = 0; slot < 13; ++slot) {
     if (slot == 8) g = pixel_rng(J, idx, iter, 2 + color);
     float4 cand = make_float4(0.f, 0.f, 0.f, 0.f);
-    const bool have = inside && (slot < 8 ? propagation_candidate(J, x, y, slot, rx, ry, ifx, ify, cur, last, &cand)
-                                          : refinement_candidate(J, g, slot - 8, cur, rx, ry, scale, span, &cand));
+    const bool have =
+        inside && (slot < 8 ? propagation_candidate(J, x, y, slot, rx, ry, ifx, ify, cur, last, &cand)
+                            : refinement_candidate(J, g, slot - 8, cur, rx, ry, scale, span, &cand) &&
+                                  exploring(J, slot - 8, iter));
     const HypCost c = eval_plane_hyp_staged<H>(J, pc, x, y, rx, ry, cand, have, rw, ref, counts,
                                                J.prune ? cur_cost : kCostInf, wb);
     if (have && c.cost < cur_cost) {

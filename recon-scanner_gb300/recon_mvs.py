@@ -83,7 +83,8 @@ class Options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("storage", C.c_int32), ("best_k", C.c_int32), ("refine", C.c_int32),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("sampling", C.c_int32), ("prefilter", C.c_int32),
                 ("interp", C.c_int32), ("tile_rows", C.c_int32), ("per_view", C.c_int32),
-                ("exhaustive", C.c_int32), ("coarse_iterations", C.c_int32), ("window_staging", C.c_int32)]
+                ("exhaustive", C.c_int32), ("coarse_iterations", C.c_int32), ("window_staging", C.c_int32),
+                ("exploration_iterations", C.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
