@@ -760,7 +760,8 @@ def sweep_profile(workload, args):
         prof = json.load(f).get("k_plane_sweep", {}).get(workload)
     if not prof:
         return {"applies": False, "why": f"no committed profile for workload {workload}"}
-    form = {"fp16": bool(args.fp16), "interp": int(args.interp), "per_view": bool(args.per_view)}
+    form = {"fp16": bool(args.fp16), "interp": int(args.interp), "per_view": bool(args.per_view),
+            "coarse": int(args.coarse), "exploration": int(args.exploration)}
     digest = kernel_sources_digest()
     out = dict(prof)
     out["sources_digest_now"] = digest
