@@ -1529,6 +1529,8 @@ typedef struct {
   int stage; /* 0 init, 1 sweep, 2 refine */
   int color, iter;
   int prune; /* 1: the engine's exact shortcuts (stop a hopeless candidate, skip a repeated one) */
+  int explore_iters; /* the engine's exploration schedule: 0 = the random and fronto-parallel candidates in
+                        every iteration; n > 0 = in iterations < n only (drawn either way) */
   int y0, y1;
 } pm_task;
 
@@ -1642,6 +1644,7 @@ static void pm_pixel(const pm_task* T, int x, int y) {
         if (q & 1) rho = cur[0] + 0.25 * span * scale * pm_sym(&g);
         if (q & 2) pm_perturb_normal(&g, rx, ry, 0.5 * scale, n);
       }
+      if ((q == 0 || q == 4) && T->explore_iters > 0 && T->iter >= T->explore_iters) continue;
       int32_t sup;
       const double c = pm_eval(T, x, y, rho, n, &sup, cur_cost);
       if (c < cur_cost) {
@@ -1745,6 +1748,12 @@ uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t
 
 uint32_t orc_plane_patchmatch_ex(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
                                  int32_t refine, int32_t prune, float* depth, float* normal, float* cost_out) {
+  return orc_plane_patchmatch_ex2(v, cfg, best_k, seed, refine, prune, 0, depth, normal, cost_out);
+}
+
+uint32_t orc_plane_patchmatch_ex2(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                                  int32_t refine, int32_t prune, int32_t explore_iters, float* depth, float* normal,
+                                  float* cost_out) {
   const size_t n = (size_t)v->ref_w * v->ref_h;
   for (size_t i = 0; i < n; ++i) {
     depth[i] = NAN;
@@ -1761,6 +1770,7 @@ uint32_t orc_plane_patchmatch_ex(const orc_views* v, const orc_config* cfg, int3
   T.best_k = best_k;
   T.seed = seed;
   T.prune = prune != 0;
+  T.explore_iters = explore_iters;
   T.rho_min = inv_min;
   T.rho_max = inv_max;
   T.inv_per_px = 1.0 / (0.5 * (k->fx + k->fy) * baseline);

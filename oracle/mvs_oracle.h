@@ -238,6 +238,13 @@ uint32_t orc_plane_patchmatch(const orc_views* v, const orc_config* cfg, int32_t
  * ones prune = 0 gives. */
 uint32_t orc_plane_patchmatch_ex(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
                                  int32_t refine, int32_t prune, float* depth, float* normal, float* cost);
+/* The same with the engine's exploration schedule (options.exploration_iterations):
+ * explore_iters > 0 evaluates the random and fronto-parallel refinement
+ * candidates only in iterations < explore_iters (they are drawn either way,
+ * so the random streams are those of the full schedule); 0 = every iteration. */
+uint32_t orc_plane_patchmatch_ex2(const orc_views* v, const orc_config* cfg, int32_t best_k, uint64_t seed,
+                                  int32_t refine, int32_t prune, int32_t explore_iters, float* depth, float* normal,
+                                  float* cost);
 
 /* Geometric consistency (spec: shaders/vulkan/recon_mvs_consistency.comp:94-140
  * with the strict transform of shaders/common/gpu_algo.h:537-538, plus a

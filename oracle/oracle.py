@@ -257,6 +257,9 @@ def load(which: str = "oracle") -> "Checker":
         lib.orc_plane_patchmatch_ex.restype = C.c_uint32
         lib.orc_plane_patchmatch_ex.argtypes = [V, P, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
                                                 C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.orc_plane_patchmatch_ex2.restype = C.c_uint32
+        lib.orc_plane_patchmatch_ex2.argtypes = [V, P, C.c_int32, C.c_uint64, C.c_int32, C.c_int32, C.c_int32,
+                                                 C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.orc_tsdf_dims.argtypes = [C.POINTER(TsdfConfig), C.POINTER(C.c_int32)]
         lib.orc_tsdf_integrate.restype = C.c_uint32
         lib.orc_tsdf_integrate.argtypes = [C.POINTER(TsdfConfig), C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -541,16 +544,19 @@ class Checker:
                                  int(half_pixel))
         return cost, vv, view_cost
 
-    def plane_patchmatch(self, vs: ViewSet, cfg: Config, best_k=4, seed=0x5DEECE66D, refine=1, prune=False):
+    def plane_patchmatch(self, vs: ViewSet, cfg: Config, best_k=4, seed=0x5DEECE66D, refine=1, prune=False,
+                         explore=0):
         """The plane-mode search with FP64 costs (prune: with the engine's
-        exact shortcuts).  Returns (filled, depth, normal HxWx3, cost)."""
+        exact shortcuts; explore: the engine's exploration schedule, 0 =
+        every iteration).  Returns (filled, depth, normal HxWx3, cost)."""
         h, w = vs.ref.shape
         depth = np.zeros((h, w), np.float32)
         normal = np.zeros((h, w, 3), np.float32)
         cost = np.zeros((h, w), np.float32)
-        filled = self.lib.orc_plane_patchmatch_ex(C.byref(vs.struct), C.byref(cfg), int(best_k), int(seed),
-                                                  int(refine), int(bool(prune)), _ptr(depth, C.c_float),
-                                                  _ptr(normal, C.c_float), _ptr(cost, C.c_float))
+        filled = self.lib.orc_plane_patchmatch_ex2(C.byref(vs.struct), C.byref(cfg), int(best_k), int(seed),
+                                                   int(refine), int(bool(prune)), int(explore),
+                                                   _ptr(depth, C.c_float), _ptr(normal, C.c_float),
+                                                   _ptr(cost, C.c_float))
         return int(filled), depth, normal, cost
 
     def bgra_to_gray(self, bgra):

@@ -129,3 +129,26 @@ def test_exact_shortcuts_leave_the_fp64_search_unchanged(orc, scene, best_k):
     assert full[0] == fast[0] > 0.5 * sc.ref.depth.size
     for a, b in zip(full[1:], fast[1:]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_exploration_schedule_in_the_fp64_search(orc, scene):
+    """The engine's exploration schedule restated in the FP64 search: a
+    cutoff at the iteration count is the full schedule bit for bit (the
+    exploration candidates are drawn either way); an early cutoff keeps the
+    maps' accuracy against analytic truth."""
+    sc = scene
+    c = O.make_config(min_depth_m=sc.min_depth, max_depth_m=sc.max_depth, iterations=4, patch_size=11,
+                      subpixel_iterations=3, num_threads=4)
+    full = orc.plane_patchmatch(views(sc), c, best_k=3, refine=1, prune=True)
+    late = orc.plane_patchmatch(views(sc), c, best_k=3, refine=1, prune=True, explore=4)
+    for a, b in zip(full, late):
+        np.testing.assert_array_equal(a, b)
+    early = orc.plane_patchmatch(views(sc), c, best_k=3, refine=1, prune=True, explore=2)
+    assert early[0] >= 0.98 * full[0]
+    truth = sc.ref.depth
+
+    def med(d):
+        ok = np.isfinite(d) & np.isfinite(truth)
+        return float(np.median(np.abs(d[ok] - truth[ok]) / truth[ok]))
+
+    assert med(early[1]) <= 1.5 * med(full[1])
